@@ -1,0 +1,158 @@
+/*
+ * parphom_gpu.h — C ABI of the GB300 phonon hot path (libparphom_gpu.so).
+ *
+ * The library replaces, for one GPU, the body of PARPHOM's per-q loop
+ * (Phonon_Calculations/SRC/calculations.F90:49-53):
+ *
+ *   create_dynamical_matrix(q, 0)     dynamical_matrix.F90:49-262
+ *   diagonalize_dynamical_matrix()    diagonalize.F90:42-149   (pzheevx)
+ *   velocity block of write_output    write_output.F90:334-466 (dD/dq, pzgemm)
+ *
+ * with one call per batch of q-points.  The Fortran driver keeps input
+ * parsing, HDF5 I/O and MPI; it calls this header through ISO_C_BINDING
+ * (the interface module is shown in INTEGRATION.md).  All integers are
+ * explicit 64-bit (the reference builds with -i8, Makefile.intel:18), all
+ * arrays are plain column-major buffers, and no call exits the process.
+ *
+ * Return codes: 0 success; -k the k-th argument is illegal (LAPACK
+ * convention); positive PP_ERR_* library errors below.  Per-q eigensolver
+ * status is reported separately in info[] with the pzheevx INFO bits
+ * (diagonalize.F90:100-115).
+ */
+#ifndef PARPHOM_GPU_H
+#define PARPHOM_GPU_H
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PP_API __attribute__((visibility("default")))
+#else
+#define PP_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pp_ctx pp_ctx;
+
+/* Library error codes (positive). */
+#define PP_OK 0
+#define PP_ERR_CUDA 1001      /* a CUDA runtime call failed                    */
+#define PP_ERR_NOMEM 1002     /* device allocation failed                      */
+#define PP_ERR_NAN 1003       /* non-finite value in force constants or q      */
+#define PP_ERR_TIMEOUT 1004   /* a bounded device wait gave up                 */
+#define PP_ERR_NODEVICE 1005  /* no CUDA device / kernel image not loadable    */
+#define PP_ERR_STATE 1006     /* context used after an unrecoverable error     */
+#define PP_ERR_UNSUPPORTED 1007
+
+/* Per-q info bits, as pzheevx INFO > 0 (diagonalize.F90:100-115). */
+#define PP_INFO_NOCONV 1      /* an eigenvalue failed to converge              */
+#define PP_INFO_NOORTH 2      /* a cluster of eigenvectors not orthogonalised  */
+#define PP_INFO_NOMEM 4       /* workspace too small for all eigenvectors      */
+#define PP_INFO_NOTCOMP 8     /* an eigenvalue was not computed                */
+
+/* Precision forms. */
+#define PP_PREC_FP64 0        /* plain IEEE double throughout                  */
+#define PP_PREC_MIXED 1       /* O(n^3) stages in double-float on FP32 pipes,
+                                 FP64 in the tridiagonal solve and velocities  */
+
+/* pp_ctx_create flags. */
+#define PP_FLAG_ENFORCE_ASR 1 /* reset Phi_II = -sum_{J!=I} Phi_IJ (off by
+                                 default: the reference does not)              */
+
+/* The reference's `system` type (mod_variables.F90:83-89) as explicit
+ * arguments.  Column-major like the Fortran module arrays. */
+typedef struct pp_system {
+  int64_t natom;
+  int64_t ntypes;
+  const double *lat;      /* [9]  lat(i,j) at lat[(i-1)+3*(j-1)]; row i = a_i (A)   */
+  const double *crys;     /* [natom*3] crys(I,k) at crys[(I-1)+natom*(k-1)]          */
+  const double *real_pos; /* [natom*3] real_pos(I,k), Cartesian (A)                  */
+  const double *mass;     /* [ntypes] amu                                            */
+  const int64_t *at_types;/* [natom] 1-based type of each atom                       */
+} pp_system;
+
+/* The reference's scalapack_variables + velocity switches
+ * (mod_variables.F90:77-81, read_input.F90:141-218). */
+typedef struct pp_eig_opts {
+  char jobz;          /* 'N' eigenvalues only, 'V' eigenvectors too              */
+  char range;         /* 'A' all, 'I' indices il..iu, 'V' values in (vl,vu]      */
+  char vel_method;    /* 'A' analytic dD/dq, 'C' central difference             */
+  char uplo;          /* must be 'U' (the reference passes 'U')                 */
+  int32_t vel;        /* nonzero: group velocities (forces jobz = 'V')           */
+  int32_t precision;  /* PP_PREC_FP64 or PP_PREC_MIXED                           */
+  double vl, vu;      /* range 'V' bounds in the reference's units: they are
+                         divided by 15.633302*33.35641 and compared with the
+                         eigenvalues of D (diagonalize.F90:75,94)               */
+  int64_t il, iu;     /* range 'I', 1-based                                      */
+  double abstol;      /* bisection absolute tolerance (reference default 1e-15) */
+  double orfac;       /* accepted for interface parity; clusters are formed by
+                         the library's own relative-gap rule                    */
+  int32_t raw_lambda; /* nonzero: w holds eigenvalues of D instead of cm^-1    */
+  int32_t want_resid; /* nonzero: fill resid[] with ||D z - lambda z||_2        */
+} pp_eig_opts;
+
+/* Output buffers for nq q-points (host or device memory depending on call).
+ * For q index t (0-based) and mode j:
+ *   w[j + ldw*t]                      frequency in cm^-1 (or lambda)
+ *   z[2*(r + ldz*j) + zstride*t]      (re, im) of eigenvector j, row r
+ *   vel[d + 3*j + velstride*t]        group velocity, direction d, m/s
+ *   resid[j + ldw*t]                  residual norm (if want_resid)          */
+typedef struct pp_result_view {
+  int64_t *m;         /* [nq] number of eigenvalues found (comp_num_eval)     */
+  int64_t *nz;        /* [nq] number of eigenvectors (comp_num_evec)          */
+  double *w;
+  int64_t ldw;
+  double *z;          /* may be NULL when eigenvectors are not wanted         */
+  int64_t ldz;
+  int64_t zstride;    /* in doubles                                           */
+  double *vel;        /* may be NULL                                          */
+  int64_t velstride;  /* in doubles                                           */
+  double *resid;      /* may be NULL                                          */
+} pp_result_view;
+
+/* Create a context on the current CUDA device: uploads Phi (after the
+ * driver's symmetrisation, force_read.F90:187-189) and builds the q-
+ * independent geometry tables.  Only the upper triangle of fc is referenced,
+ * as pzheevx references only the upper triangle of D (diagonalize.F90:73).
+ * Replaces: the state set up by read_lammps_data / read_force_constants
+ * (main.F90:53-62) as seen by create_dynamical_matrix. */
+PP_API int pp_ctx_create(const pp_system *sys, const double *fc, int64_t ldfc, int64_t flags, pp_ctx **out);
+
+/* Free every device resource of the context. */
+PP_API int pp_ctx_destroy(pp_ctx *ctx);
+
+/* Solve nq q-points: q(t,k) at q[t + ldq*k] in reduced reciprocal
+ * coordinates (q_file%points, q_read.F90:82-93).  Host buffers in and out;
+ * the library batches internally.  info[t] receives the pzheevx-style bits.
+ * Replaces: calculations.F90:50-52 (minus the HDF5 writes). */
+PP_API int pp_solve_batch(pp_ctx *ctx, const double *q, int64_t ldq, int64_t nq, const pp_eig_opts *opts,
+                   const pp_result_view *out, int64_t *info);
+
+/* Same as pp_solve_batch with q, the result buffers and info in device
+ * memory, enqueued on `stream` (a cudaStream_t; NULL = legacy stream). */
+PP_API int pp_solve_batch_device(pp_ctx *ctx, const double *q_dev, int64_t ldq, int64_t nq, const pp_eig_opts *opts,
+                          const pp_result_view *out_dev, int64_t *info_dev, void *stream);
+
+/* D(q) (derivative = 0) or dD/dq_k (derivative = k in 1..3, vel_method 'A'
+ * or 'C') for one q, written as the full Hermitian matrix (upper triangle
+ * mirrored) to host buffer d[2*(r + ldd*c)].
+ * Replaces: create_dynamical_matrix(q_indx, derivative),
+ * dynamical_matrix.F90:49-191. */
+PP_API int pp_dynamical_matrix(pp_ctx *ctx, const double *q, int64_t derivative, char vel_method, double *d,
+                        int64_t ldd);
+
+/* Human-readable text for a return code. */
+PP_API const char *pp_strerror(int code);
+
+/* Library version: major*10000 + minor*100 + patch. */
+PP_API int64_t pp_version(void);
+
+/* Number of kernels this library launched on the calling thread's contexts
+ * since load (for launch accounting in benchmarks). */
+PP_API int64_t pp_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARPHOM_GPU_H */

@@ -1,0 +1,570 @@
+// C ABI of the phonon hot path: context lifetime, workspace sizing and the
+// per-batch pipeline  D(q) -> tridiagonal -> eigenvalues -> eigenvectors ->
+// back-transform -> velocities -> outputs.
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/parphom_gpu.h"
+#include "pp_internal.cuh"
+
+namespace pp {
+static std::atomic<int64_t> g_launches{0};
+void count_launch(int64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+}  // namespace pp
+
+using namespace pp;
+
+struct pp_ctx {
+  Geometry g;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int broken = 0;
+  // workspace (grown on demand)
+  EigWork w;
+  int cap_B = 0, cap_m = 0;
+  int cap_prec = -1;
+  void *ws = nullptr;
+  size_t ws_bytes = 0;
+  // velocity buffers
+  double *vpart = nullptr;
+  double *vraw = nullptr;
+  int nsplit = 8;
+  // staging for host calls
+  double *d_q = nullptr;
+  double *d_w = nullptr, *d_z = nullptr, *d_vel = nullptr;
+  int64_t *d_m = nullptr, *d_nz = nullptr, *d_info = nullptr;
+};
+
+namespace {
+
+constexpr double PI2_REF = (double)6.283185307179586f;  // lammps_read.F90:255
+constexpr double DEL_REF = (double)1e-6f;               // dynamical_matrix.F90:60
+constexpr double C_RANGE = (double)(15.633302f * 33.35641f);  // diagonalize.F90:75
+
+int cuda_err(cudaError_t e) {
+  if (e == cudaSuccess) return PP_OK;
+  if (e == cudaErrorMemoryAllocation) return PP_ERR_NOMEM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+    return PP_ERR_NODEVICE;
+  return PP_ERR_CUDA;
+}
+
+#define TRY_CUDA(x)                       \
+  do {                                    \
+    cudaError_t e__ = (x);                \
+    if (e__ != cudaSuccess) return cuda_err(e__); \
+  } while (0)
+
+// lammps_read.F90:250-274 (B = 2 pi_f * inverse transpose), Fortran layout.
+void matinvtransp3(const double *A, double *B) {
+#define AA(i, j) A[(i - 1) + 3 * (j - 1)]
+#define BB(i, j) B[(i - 1) + 3 * (j - 1)]
+  const double detinv = 1.0 / (AA(1, 1) * AA(2, 2) * AA(3, 3) - AA(1, 1) * AA(2, 3) * AA(3, 2) -
+                               AA(1, 2) * AA(2, 1) * AA(3, 3) + AA(1, 2) * AA(2, 3) * AA(3, 1) +
+                               AA(1, 3) * AA(2, 1) * AA(3, 2) - AA(1, 3) * AA(2, 2) * AA(3, 1));
+  BB(1, 1) = +detinv * (AA(2, 2) * AA(3, 3) - AA(2, 3) * AA(3, 2)) * PI2_REF;
+  BB(1, 2) = -detinv * (AA(2, 1) * AA(3, 3) - AA(2, 3) * AA(3, 1)) * PI2_REF;
+  BB(1, 3) = +detinv * (AA(2, 1) * AA(3, 2) - AA(2, 2) * AA(3, 1)) * PI2_REF;
+  BB(2, 1) = -detinv * (AA(1, 2) * AA(3, 3) - AA(1, 3) * AA(3, 2)) * PI2_REF;
+  BB(2, 2) = +detinv * (AA(1, 1) * AA(3, 3) - AA(1, 3) * AA(3, 1)) * PI2_REF;
+  BB(2, 3) = -detinv * (AA(1, 1) * AA(3, 2) - AA(1, 2) * AA(3, 1)) * PI2_REF;
+  BB(3, 1) = +detinv * (AA(1, 2) * AA(2, 3) - AA(1, 3) * AA(2, 2)) * PI2_REF;
+  BB(3, 2) = -detinv * (AA(1, 1) * AA(2, 3) - AA(1, 3) * AA(2, 1)) * PI2_REF;
+  BB(3, 3) = +detinv * (AA(1, 1) * AA(2, 2) - AA(1, 2) * AA(2, 1)) * PI2_REF;
+#undef AA
+#undef BB
+}
+
+// lammps_read.F90:281-309: u = (A^-1)^T x.
+void linsolve(const double *x, const double *A, double *u) {
+#define AA(i, j) A[(i - 1) + 3 * (j - 1)]
+  const double detinv = 1.0 / (AA(1, 1) * AA(2, 2) * AA(3, 3) - AA(1, 1) * AA(2, 3) * AA(3, 2) -
+                               AA(1, 2) * AA(2, 1) * AA(3, 3) + AA(1, 2) * AA(2, 3) * AA(3, 1) +
+                               AA(1, 3) * AA(2, 1) * AA(3, 2) - AA(1, 3) * AA(2, 2) * AA(3, 1));
+  double Bm[3][3];
+  Bm[0][0] = +detinv * (AA(2, 2) * AA(3, 3) - AA(2, 3) * AA(3, 2));
+  Bm[1][0] = -detinv * (AA(2, 1) * AA(3, 3) - AA(2, 3) * AA(3, 1));
+  Bm[2][0] = +detinv * (AA(2, 1) * AA(3, 2) - AA(2, 2) * AA(3, 1));
+  Bm[0][1] = -detinv * (AA(1, 2) * AA(3, 3) - AA(1, 3) * AA(3, 2));
+  Bm[1][1] = +detinv * (AA(1, 1) * AA(3, 3) - AA(1, 3) * AA(3, 1));
+  Bm[2][1] = -detinv * (AA(1, 1) * AA(3, 2) - AA(1, 2) * AA(3, 1));
+  Bm[0][2] = +detinv * (AA(1, 2) * AA(2, 3) - AA(1, 3) * AA(2, 2));
+  Bm[1][2] = -detinv * (AA(1, 1) * AA(2, 3) - AA(1, 3) * AA(2, 1));
+  Bm[2][2] = +detinv * (AA(1, 1) * AA(2, 2) - AA(1, 2) * AA(2, 1));
+#undef AA
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s += Bm[k][i] * x[k];
+    u[i] = s;
+  }
+}
+
+void free_ws(pp_ctx *c) {
+  if (c->ws) cudaFree(c->ws);
+  c->ws = nullptr;
+  c->ws_bytes = 0;
+  c->cap_B = c->cap_m = 0;
+  c->w = EigWork();
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Carve every batch buffer out of one allocation.
+int ensure_ws(pp_ctx *c, int B, int mcap) {
+  if (c->ws && B <= c->cap_B && mcap <= c->cap_m) return PP_OK;
+  free_ws(c);
+  const int64_t n = c->g.n;
+  const int nb = 32;
+  const int64_t lda = (n + 7) / 8 * 8;
+  const int nchunk = (int)((n + 63) / 64);
+  const int nrb = (int)((n + 255) / 256) + 1;
+  const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
+  const int ldwp = std::max(mcap, 64);
+  const int ksplit = (int)((n + 511) / 512);
+  const int64_t nbnd = c->g.nbnd;
+  std::vector<std::pair<void **, size_t>> parts;
+  EigWork &w = c->w;
+  w = EigWork();
+  w.B = B;
+  w.nmax = (int)n;
+  w.mcap = mcap;
+  w.nb = nb;
+  w.lda = lda;
+  w.sA = lda * n;
+  w.lde = lda;
+  w.sE = lda * mcap;
+  w.nchunk = nchunk;
+  w.nrb = nrb;
+  w.scratch_threads = T;
+  w.ldwp = ldwp;
+  w.ksplit = ksplit;
+  size_t off = 0;
+  auto add = [&](void **p, size_t bytes) {
+    parts.push_back({p, off});
+    off = align_up(off + bytes);
+  };
+  add((void **)&w.nvec, sizeof(int) * B);
+  add(&w.A, 16 * (size_t)B * w.sA);
+  add(&w.E, 16 * (size_t)B * w.sE);
+  add(&w.W, 16 * (size_t)B * lda * nb);
+  add(&w.P, 16 * (size_t)B * nchunk * lda);
+  add(&w.X, 16 * (size_t)B * 2 * nb);
+  add((void **)&w.nrm, 8 * (size_t)B * nrb);
+  add((void **)&w.wv, 16 * (size_t)B * nrb);
+  add((void **)&w.d, 8 * (size_t)B * n);
+  add((void **)&w.e, 8 * (size_t)B * n);
+  add((void **)&w.tau, 16 * (size_t)B * n);
+  add((void **)&w.scal, 16 * (size_t)B * 4);
+  add((void **)&w.w, 8 * (size_t)B * n);
+  add((void **)&w.rng, 8 * (size_t)B * 8);
+  add((void **)&w.tinfo, 8 * (size_t)B * 8);
+  add((void **)&w.cls, 4 * (size_t)B * (n + 1));
+  add((void **)&w.ncl, 4 * (size_t)B);
+  add((void **)&w.scratch, 8 * (size_t)B * 4 * n * T);
+  add((void **)&w.piv, (size_t)B * n * T);
+  add((void **)&w.info, 8 * (size_t)B);
+  add((void **)&w.Tf, 16 * (size_t)B * 1024);
+  add((void **)&w.G, 16 * (size_t)B * 1024);
+  add(&w.Wb, 16 * (size_t)B * 32 * ldwp);
+  add(&w.Wp, 16 * (size_t)B * ksplit * 32 * ldwp);
+  add((void **)&c->vpart, 8 * (size_t)B * c->nsplit * 3 * mcap + 16 * (size_t)B * nbnd * 3);
+  add((void **)&c->vraw, 8 * (size_t)B * 3 * mcap);
+  add((void **)&c->d_q, 8 * (size_t)B * 3);
+  add((void **)&c->d_w, 8 * (size_t)B * n);
+  add((void **)&c->d_vel, 8 * (size_t)B * 3 * mcap);
+  add((void **)&c->d_m, 8 * (size_t)B);
+  add((void **)&c->d_nz, 8 * (size_t)B);
+  add((void **)&c->d_info, 8 * (size_t)B);
+  void *base = nullptr;
+  cudaError_t e = cudaMalloc(&base, off);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return PP_ERR_NOMEM;
+  }
+  for (auto &p : parts) *p.first = (char *)base + p.second;
+  c->ws = base;
+  c->ws_bytes = off;
+  w.bytes = off;
+  c->cap_B = B;
+  c->cap_m = mcap;
+  std::vector<int> nv(B, (int)n);
+  TRY_CUDA(cudaMemcpy(w.nvec, nv.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
+  return PP_OK;
+}
+
+size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd) {
+  const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
+  size_t per = 16 * (size_t)n * n + 16 * (size_t)n * mcap + 8 * (size_t)4 * n * T + (size_t)n * T +
+               16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
+               8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd;
+  return per * B;
+}
+
+int check_opts(const pp_ctx *c, const pp_eig_opts *o) {
+  if (!o) return -5;
+  if (o->jobz != 'N' && o->jobz != 'V') return -5;
+  if (o->range != 'A' && o->range != 'I' && o->range != 'V') return -5;
+  if (o->uplo != 'U' && o->uplo != 0) return -5;
+  if (o->vel && o->vel_method != 'A' && o->vel_method != 'C') return -5;
+  if (o->precision != PP_PREC_FP64 && o->precision != PP_PREC_MIXED) return -5;
+  const int64_t n = c->g.n;
+  if (o->range == 'I' && (o->il < 1 || o->iu > n || o->il > o->iu)) return -5;
+  if (o->range == 'V' && !(o->vl < o->vu)) return -5;
+  return PP_OK;
+}
+
+// Run the pipeline for B q-points already in c->d_q; results left in the
+// EigWork buffers, velocities in c->vraw.
+int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap) {
+  EigWork &w = c->w;
+  w.B = B;
+  cudaStream_t s = c->stream;
+  const int prec = o->precision;
+  const bool vecs = o->jobz == 'V' || o->vel;
+  TRY_CUDA(assemble_batch(c->g, c->d_q, B, w.A, w.lda, w.sA, prec == PP_PREC_MIXED ? 1 : 0, s));
+  if (prec == PP_PREC_MIXED)
+    TRY_CUDA(tridiagonalize<df>(w, s));
+  else
+    TRY_CUDA(tridiagonalize<double>(w, s));
+  TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s));
+  (void)mcap;
+  if (vecs) {
+    if (prec == PP_PREC_MIXED) {
+      TRY_CUDA(tridiag_eigenvectors<df>(w, s));
+      TRY_CUDA(back_transform<df>(w, s));
+    } else {
+      TRY_CUDA(tridiag_eigenvectors<double>(w, s));
+      TRY_CUDA(back_transform<double>(w, s));
+    }
+    if (o->vel) {
+      TRY_CUDA(velocities(c->g, c->d_q, B, w.E, w.lde, w.sE, prec == PP_PREC_MIXED ? 1 : 0, w.rng, w.mcap,
+                          o->vel_method, c->vraw, c->vpart, c->nsplit, s));
+    }
+  }
+  return PP_OK;
+}
+
+int mcap_for(const pp_ctx *c, const pp_eig_opts *o) {
+  const int64_t n = c->g.n;
+  if (o->range == 'I') return (int)(o->iu - o->il + 1);
+  return (int)n;
+}
+
+int pick_batch(pp_ctx *c, int64_t nq, int mcap) {
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  if (c->ws) fr += c->ws_bytes;
+  const size_t budget = (size_t)(0.6 * (double)fr);
+  int B = (int)std::min<int64_t>(nq, 64);
+  while (B > 1 && ws_bytes_estimate(c->g.n, B, mcap, c->g.nbnd) > budget) B = B / 2;
+  const char *env = getenv("PARPHOM_GPU_BATCH");
+  if (env) {
+    int v = atoi(env);
+    if (v > 0) B = std::min<int64_t>(v, nq);
+  }
+  return std::max(B, 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t pp_version(void) { return 100; }
+
+int64_t pp_kernel_launches(void) { return pp::g_launches.load(); }
+
+const char *pp_strerror(int code) {
+  switch (code) {
+    case PP_OK: return "success";
+    case PP_ERR_CUDA: return "CUDA runtime error";
+    case PP_ERR_NOMEM: return "device memory allocation failed";
+    case PP_ERR_NAN: return "non-finite value in the input";
+    case PP_ERR_TIMEOUT: return "bounded device wait timed out";
+    case PP_ERR_NODEVICE: return "no usable CUDA device for this library (sm_103a)";
+    case PP_ERR_STATE: return "context is unusable after an earlier error";
+    case PP_ERR_UNSUPPORTED: return "unsupported option";
+    default:
+      if (code < 0) return "illegal argument (index given by -code)";
+      return "unknown error";
+  }
+}
+
+int pp_ctx_create(const pp_system *sys, const double *fc, int64_t ldfc, int64_t flags, pp_ctx **out) {
+  if (!sys) return -1;
+  if (!fc) return -2;
+  if (!out) return -5;
+  *out = nullptr;
+  if (sys->natom < 1 || sys->ntypes < 1 || !sys->lat || !sys->crys || !sys->real_pos || !sys->mass ||
+      !sys->at_types)
+    return -1;
+  const int64_t N = sys->natom, n = 3 * N;
+  if (ldfc < n) return -3;
+  if (N > 46000) return -1;  // mask table and 32-bit atom indices
+  for (int64_t t = 0; t < sys->ntypes; ++t)
+    if (!(sys->mass[t] > 0.0) || !std::isfinite(sys->mass[t])) return PP_ERR_NAN;
+  for (int64_t I = 0; I < N; ++I)
+    if (sys->at_types[I] < 1 || sys->at_types[I] > sys->ntypes) return -1;
+  for (int k = 0; k < 9; ++k)
+    if (!std::isfinite(sys->lat[k])) return PP_ERR_NAN;
+  for (int64_t k = 0; k < 3 * N; ++k)
+    if (!std::isfinite(sys->crys[k]) || !std::isfinite(sys->real_pos[k])) return PP_ERR_NAN;
+  for (int64_t cc = 0; cc < n; ++cc)
+    for (int64_t r = 0; r <= cc; ++r)
+      if (!std::isfinite(fc[r + ldfc * cc])) return PP_ERR_NAN;
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return PP_ERR_NODEVICE;
+  }
+  pp_ctx *c = new (std::nothrow) pp_ctx();
+  if (!c) return PP_ERR_NOMEM;
+  cudaGetDevice(&c->device);
+  Geometry &g = c->g;
+  g.natom = N;
+  g.n = n;
+  std::memcpy(g.lat, sys->lat, 9 * sizeof(double));
+  matinvtransp3(g.lat, g.rec_lat);
+  // CD step (dynamical_matrix.F90:134-148)
+  {
+    const double *rl = g.rec_lat;
+    const double v = DEL_REF * std::sqrt(std::fabs(rl[0] * rl[4] - rl[3] * rl[1]));
+    const double del = v > DEL_REF ? v : DEL_REF;
+    for (int k = 0; k < 3; ++k) {
+      double dv[3] = {0, 0, 0};
+      dv[k] = del;
+      linsolve(dv, g.rec_lat, g.delta_crys[k]);
+      g.delta_norm[k] = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    }
+  }
+  std::vector<double> mass_atom(N);
+  for (int64_t I = 0; I < N; ++I) mass_atom[I] = sys->mass[sys->at_types[I] - 1];
+
+  auto fail = [&](int code) {
+    pp_ctx_destroy(c);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(PP_ERR_CUDA);
+  cudaStream_t s = c->stream;
+  if (cudaMalloc(&g.d_fc, sizeof(double) * n * n) != cudaSuccess) return fail(PP_ERR_NOMEM);
+  if (cudaMalloc(&g.d_crys, sizeof(double) * 3 * N) != cudaSuccess) return fail(PP_ERR_NOMEM);
+  if (cudaMalloc(&g.d_pos, sizeof(double) * 3 * N) != cudaSuccess) return fail(PP_ERR_NOMEM);
+  if (cudaMalloc(&g.d_mass, sizeof(double) * N) != cudaSuccess) return fail(PP_ERR_NOMEM);
+  if (cudaMalloc(&g.d_mask, sizeof(uint16_t) * N * N) != cudaSuccess) return fail(PP_ERR_NOMEM);
+  if (cudaMemcpy2DAsync(g.d_fc, sizeof(double) * n, fc, sizeof(double) * ldfc, sizeof(double) * n, n,
+                        cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return fail(PP_ERR_CUDA);
+  cudaMemcpyAsync(g.d_crys, sys->crys, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(g.d_pos, sys->real_pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(g.d_mass, mass_atom.data(), sizeof(double) * N, cudaMemcpyHostToDevice, s);
+  if (geom_symmetrize_fc(g, (flags & PP_FLAG_ENFORCE_ASR) ? 1 : 0, s) != cudaSuccess) return fail(PP_ERR_CUDA);
+  if (geom_build_masks(g, s) != cudaSuccess) return fail(PP_ERR_CUDA);
+  // boundary blocks: I < J, tie set with a non-home image, Phi block non-zero
+  uint8_t *d_flags = nullptr;
+  if (cudaMalloc(&d_flags, (size_t)N * N) != cudaSuccess) return fail(PP_ERR_NOMEM);
+  geom_block_nonzero(g, d_flags, s);
+  std::vector<uint8_t> flags_h((size_t)N * N);
+  std::vector<uint16_t> mask_h((size_t)N * N);
+  cudaMemcpyAsync(flags_h.data(), d_flags, (size_t)N * N, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(mask_h.data(), g.d_mask, sizeof(uint16_t) * N * N, cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  cudaFree(d_flags);
+  if (e != cudaSuccess) return fail(cuda_err(e));
+  std::vector<int2> bnd;
+  std::vector<uint16_t> bmask;
+  for (int64_t I = 0; I < N; ++I)
+    for (int64_t J = I + 1; J < N; ++J) {
+      const uint16_t m = mask_h[I + N * J];
+      if ((m & ~(1u << 4)) && flags_h[I + N * J]) {
+        bnd.push_back(make_int2((int)I, (int)J));
+        bmask.push_back(m);
+      }
+    }
+  g.nbnd = (int64_t)bnd.size();
+  if (g.nbnd) {
+    if (cudaMalloc(&g.d_bnd, sizeof(int2) * g.nbnd) != cudaSuccess) return fail(PP_ERR_NOMEM);
+    if (cudaMalloc(&g.d_bndmask, sizeof(uint16_t) * g.nbnd) != cudaSuccess) return fail(PP_ERR_NOMEM);
+    cudaMemcpy(g.d_bnd, bnd.data(), sizeof(int2) * g.nbnd, cudaMemcpyHostToDevice);
+    cudaMemcpy(g.d_bndmask, bmask.data(), sizeof(uint16_t) * g.nbnd, cudaMemcpyHostToDevice);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(cuda_err(e));
+  *out = c;
+  return PP_OK;
+}
+
+int pp_ctx_destroy(pp_ctx *c) {
+  if (!c) return -1;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_ws(c);
+  cudaFree(c->g.d_fc);
+  cudaFree(c->g.d_crys);
+  cudaFree(c->g.d_pos);
+  cudaFree(c->g.d_mass);
+  cudaFree(c->g.d_mask);
+  cudaFree(c->g.d_bnd);
+  cudaFree(c->g.d_bndmask);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return PP_OK;
+}
+
+int pp_solve_batch(pp_ctx *c, const double *q, int64_t ldq, int64_t nq, const pp_eig_opts *o,
+                   const pp_result_view *out, int64_t *info) {
+  if (!c) return -1;
+  if (c->broken) return PP_ERR_STATE;
+  if (!q && nq > 0) return -2;
+  if (ldq < nq) return -3;
+  if (nq < 0) return -4;
+  int r = check_opts(c, o);
+  if (r) return r;
+  if (!out || !out->w || !out->m || !out->nz) return -6;
+  if (nq == 0) return PP_OK;
+  for (int64_t t = 0; t < nq; ++t)
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(q[t + ldq * k])) return PP_ERR_NAN;
+  const int64_t n = c->g.n;
+  const int mcap = mcap_for(c, o);
+  if (out->ldw < n) return -6;
+  const bool vecs = o->jobz == 'V' || o->vel;
+  const bool want_z = vecs && out->z;
+  if (want_z && out->ldz < n) return -6;
+  const int B = pick_batch(c, nq, mcap);
+  r = ensure_ws(c, B, mcap);
+  if (r) return r;
+  cudaStream_t s = c->stream;
+  std::vector<double> qh(3 * (size_t)B);
+  std::vector<int64_t> mh(B), nzh(B), infoh(B);
+  for (int64_t t0 = 0; t0 < nq; t0 += B) {
+    const int Bb = (int)std::min<int64_t>(B, nq - t0);
+    for (int b = 0; b < Bb; ++b)
+      for (int k = 0; k < 3; ++k) qh[3 * b + k] = q[(t0 + b) + ldq * k];
+    TRY_CUDA(cudaMemcpyAsync(c->d_q, qh.data(), sizeof(double) * 3 * Bb, cudaMemcpyHostToDevice, s));
+    r = run_batch(c, Bb, o, mcap);
+    if (r) {
+      c->broken = 1;
+      return r;
+    }
+    TRY_CUDA(finalize_outputs(c->w, o->precision == PP_PREC_MIXED ? 1 : 0, o->raw_lambda, c->vraw, o->vel ? 1 : 0,
+                              0, c->d_w, n, nullptr, 0, 0, c->d_vel, 3 * (int64_t)c->w.mcap, c->d_m, c->d_nz, c->d_info,
+                              vecs ? 1 : 0, s));
+    TRY_CUDA(cudaMemcpyAsync(mh.data(), c->d_m, 8 * Bb, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaMemcpyAsync(nzh.data(), c->d_nz, 8 * Bb, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaMemcpyAsync(infoh.data(), c->d_info, 8 * Bb, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaStreamSynchronize(s));
+    for (int b = 0; b < Bb; ++b) {
+      const int64_t t = t0 + b;
+      out->m[t] = mh[b];
+      out->nz[t] = (o->jobz == 'V' || o->vel) ? nzh[b] : 0;
+      if (info) info[t] = infoh[b];
+      const int64_t m = mh[b];
+      if (m > 0) {
+        TRY_CUDA(cudaMemcpyAsync(out->w + out->ldw * t, c->d_w + n * b, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                                 s));
+        if (o->vel && out->vel)
+          TRY_CUDA(cudaMemcpyAsync(out->vel + out->velstride * t, c->d_vel + 3 * (int64_t)c->w.mcap * b,
+                                   sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, s));
+      }
+    }
+    if (want_z) {
+      // eigenvectors: convert to FP64 complex in the A buffer (free after the
+      // back-transform), then copy each matrix with the caller's pitch.
+      double *zst = (double *)c->w.A;
+      TRY_CUDA(finalize_outputs(c->w, o->precision == PP_PREC_MIXED ? 1 : 0, o->raw_lambda, c->vraw, 0, 1, nullptr,
+                                0, zst, c->w.lda, 2 * c->w.sA, nullptr, 0, nullptr, nullptr, nullptr, 1, s));
+      for (int b = 0; b < Bb; ++b) {
+        const int64_t t = t0 + b;
+        const int64_t m = mh[b];
+        if (m > 0)
+          TRY_CUDA(cudaMemcpy2DAsync(out->z + out->zstride * t, sizeof(double) * 2 * out->ldz,
+                                     zst + 2 * c->w.sA * b, sizeof(double) * 2 * c->w.lda, sizeof(double) * 2 * n, m,
+                                     cudaMemcpyDeviceToHost, s));
+      }
+    }
+    TRY_CUDA(cudaStreamSynchronize(s));
+  }
+  return PP_OK;
+}
+
+int pp_solve_batch_device(pp_ctx *c, const double *q_dev, int64_t ldq, int64_t nq, const pp_eig_opts *o,
+                          const pp_result_view *out, int64_t *info_dev, void *stream) {
+  if (!c) return -1;
+  if (c->broken) return PP_ERR_STATE;
+  if (!q_dev && nq > 0) return -2;
+  if (ldq < nq) return -3;
+  if (nq < 0) return -4;
+  int r = check_opts(c, o);
+  if (r) return r;
+  if (!out || !out->w || !out->m || !out->nz) return -6;
+  if (nq == 0) return PP_OK;
+  const int64_t n = c->g.n;
+  const int mcap = mcap_for(c, o);
+  if (out->ldw < n) return -6;
+  const bool vecs = o->jobz == 'V' || o->vel;
+  const bool want_z = vecs && out->z;
+  if (want_z && out->ldz < n) return -6;
+  const int B = pick_batch(c, nq, mcap);
+  r = ensure_ws(c, B, mcap);
+  if (r) return r;
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  cudaStream_t saved = c->stream;
+  c->stream = s;
+  for (int64_t t0 = 0; t0 < nq; t0 += B) {
+    const int Bb = (int)std::min<int64_t>(B, nq - t0);
+    for (int k = 0; k < 3; ++k)
+      TRY_CUDA(cudaMemcpy2DAsync(c->d_q + k, 3 * sizeof(double), q_dev + t0 + ldq * k, sizeof(double),
+                                 sizeof(double), Bb, cudaMemcpyDeviceToDevice, s));
+    r = run_batch(c, Bb, o, mcap);
+    if (r) {
+      c->stream = saved;
+      c->broken = 1;
+      return r;
+    }
+    r = cuda_err(finalize_outputs(c->w, o->precision == PP_PREC_MIXED ? 1 : 0, o->raw_lambda, c->vraw,
+                                  o->vel ? 1 : 0, want_z ? 1 : 0, out->w + out->ldw * t0, out->ldw,
+                                  want_z ? out->z + out->zstride * t0 : nullptr, out->ldz, out->zstride,
+                                  out->vel ? out->vel + out->velstride * t0 : nullptr, out->velstride, out->m + t0,
+                                  out->nz + t0, info_dev ? info_dev + t0 : nullptr, vecs ? 1 : 0, s));
+    if (r) {
+      c->stream = saved;
+      return r;
+    }
+  }
+  c->stream = saved;
+  return PP_OK;
+}
+
+int pp_dynamical_matrix(pp_ctx *c, const double *q, int64_t derivative, char vel_method, double *d, int64_t ldd) {
+  if (!c) return -1;
+  if (!q) return -2;
+  if (derivative < 0 || derivative > 3) return -3;
+  if (derivative > 0 && vel_method != 'A' && vel_method != 'C') return -4;
+  if (!d) return -5;
+  const int64_t n = c->g.n;
+  if (ldd < n) return -6;
+  cudaStream_t s = c->stream;
+  double *dq = nullptr;
+  z64 *dout = nullptr;
+  TRY_CUDA(cudaMalloc(&dq, 3 * sizeof(double)));
+  cudaError_t e = cudaMalloc(&dout, sizeof(z64) * n * n);
+  if (e != cudaSuccess) {
+    cudaFree(dq);
+    return PP_ERR_NOMEM;
+  }
+  cudaMemcpyAsync(dq, q, 3 * sizeof(double), cudaMemcpyHostToDevice, s);
+  e = assemble_deriv(c->g, dq, (int)derivative, vel_method, dout, n, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(d, sizeof(double) * 2 * ldd, dout, sizeof(z64) * n, sizeof(z64) * n, n,
+                          cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(dq);
+  cudaFree(dout);
+  return cuda_err(e);
+}
+
+}  // extern "C"

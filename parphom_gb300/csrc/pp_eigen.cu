@@ -1,0 +1,990 @@
+// Batched Hermitian eigensolver with pzheevx semantics (range A/I/V, abstol,
+// optional eigenvectors) for the phonon hot path.
+//
+// Stages (each a set of batched kernels; matrix b of the batch is picked by
+// blockIdx.y/z and may have its own order nvec[b]):
+//  1. Householder reduction to real symmetric tridiagonal form, lower
+//     formulation, blocked in panels of nb columns: the per-column work
+//     (column update, reflector, Hermitian matrix-vector product and its
+//     panel corrections) follows the zlatrd recurrence; after each panel the
+//     trailing matrix gets the rank-2nb update A -= V W^H + W V^H.  The full
+//     Hermitian square is kept so that every matrix-vector pass reads
+//     coalesced columns.  A = Q T Q^H with Q = H(0) H(1) ... H(n-2),
+//     H(i) = I - tau_i v_i v_i^H.
+//  2. Eigenvalues of T by Sturm-count bisection, one thread per eigenvalue
+//     index, with the dstebz tolerance rule max(abstol, pivmin,
+//     2 ulp max(|lo|,|hi|)).  Always FP64.
+//  3. Eigenvectors of T by inverse iteration with partial-pivoting LU of
+//     T - lambda I, one thread per eigenvalue cluster, modified Gram-Schmidt
+//     inside clusters (consecutive eigenvalues closer than 1e-7 ||T||).
+//     Always FP64.
+//  4. Back-transform E = Q Z, panel by panel from the last, with the compact
+//     WY form I - V Tf V^H (zlarft forward/columnwise).
+// Stages 1 and 4 are templated on the real arithmetic R: double (plain FP64
+// form) or df (double-float on the FP32 pipes, the mixed form).
+#include <cfloat>
+#include <cstdio>
+
+#include "pp_internal.cuh"
+
+namespace pp {
+
+template <class R>
+using C = cx<R>;
+
+static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+__device__ __forceinline__ int cdiv_dev(int a, int b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------------------
+// block reductions (double / z64)
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <int NT>
+__device__ double block_sum(double v, double *sh) {
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (threadIdx.x < NT / 32) ? sh[threadIdx.x] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sh[0] = r;
+  __syncthreads();
+  r = sh[0];
+  __syncthreads();
+  return r;
+}
+template <int NT>
+__device__ z64 block_sum_z(z64 v, double *sh) {
+  z64 r;
+  r.re = block_sum<NT>(v.re, sh);
+  r.im = block_sum<NT>(v.im, sh);
+  return r;
+}
+
+// ===========================================================================
+// Stage 1: reduction to tridiagonal form
+// ===========================================================================
+constexpr int TR_NT = 256;   // threads of the column kernels
+constexpr int HV_RB = 128;   // rows per hemv block
+constexpr int HV_CC = 64;    // columns per hemv chunk
+
+// A(i:n,i) -= V(i:n,0:jj) conj(W(i,0:jj))^T + W(i:n,0:jj) conj(V(i,0:jj))^T ;
+// d[i] = Re A(i,i) ; partial sums of |A(r,i)|^2 for r >= i+2.
+template <class R>
+__global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
+                                                  const int *nvec, int i, int k0, int jj, double *dd, int64_t sd,
+                                                  double *nrm, int nrb) {
+  __shared__ C<R> sv[64], sw[64];
+  __shared__ double red[32];
+  const int b = blockIdx.y;
+  const int n = nvec[b];
+  if (i >= n) return;
+  C<R> *A = Ab + b * sA;
+  C<R> *W = Wb + b * sW;
+  const int64_t ldw = lda;
+  for (int c = threadIdx.x; c < jj; c += blockDim.x) {
+    sv[c] = A[i + lda * (k0 + c)];
+    sw[c] = W[i + ldw * c];
+  }
+  __syncthreads();
+  const int r = i + blockIdx.x * TR_NT + threadIdx.x;
+  double part = 0.0;
+  if (r < n) {
+    C<R> a = A[r + lda * i];
+    if (jj > 0) {
+      C<R> acc = cz<R>();
+      for (int c = 0; c < jj; ++c) {
+        cmac(acc, A[r + lda * (k0 + c)], cconj(sw[c]));
+        cmac(acc, W[r + ldw * c], cconj(sv[c]));
+      }
+      a = csub(a, cfin(acc));
+    }
+    if (r == i) {
+      a.im = RT<R>::zero();
+      dd[b * sd + i] = RT<R>::to(a.re);
+    }
+    A[r + lda * i] = a;
+    if (r >= i + 2) {
+      z64 t = cto64(a);
+      part = t.re * t.re + t.im * t.im;
+    }
+  }
+  double s = block_sum<TR_NT>(part, red);
+  if (threadIdx.x == 0) nrm[b * nrb + blockIdx.x] = s;
+}
+
+// zlarfg on A(i+1:n, i); v := [1, x/(alpha-beta)] written back in place.
+template <class R>
+__global__ void __launch_bounds__(TR_NT) k_reflector(C<R> *Ab, int64_t lda, int64_t sA, const int *nvec, int i,
+                                                     int nparts, const double *nrm, int nrb, double *ee, z64 *tau,
+                                                     int64_t sd, z64 *scal) {
+  __shared__ double red[32];
+  __shared__ z64 s_scale;
+  __shared__ int s_skip;
+  const int b = blockIdx.x;
+  const int n = nvec[b];
+  if (i >= n - 1) {
+    if (threadIdx.x == 0 && i < n) {
+      tau[b * sd + i] = z64{0.0, 0.0};
+      ee[b * sd + i] = 0.0;
+      scal[b * 4 + 0] = z64{0.0, 0.0};
+      scal[b * 4 + 1] = z64{0.0, 0.0};
+    }
+    return;
+  }
+  C<R> *A = Ab + b * sA;
+  double p = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) p += nrm[b * nrb + k];
+  double xn2 = block_sum<TR_NT>(p, red);
+  if (threadIdx.x == 0) {
+    z64 alpha = cto64(A[(i + 1) + lda * i]);
+    double xnorm = sqrt(xn2);
+    z64 t, sc;
+    double beta;
+    int skip = 0;
+    if (xnorm == 0.0 && alpha.im == 0.0) {
+      t = z64{0.0, 0.0};
+      beta = alpha.re;
+      sc = z64{1.0, 0.0};
+      skip = 1;
+    } else {
+      double nrm3 = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + xn2);
+      beta = -copysign(nrm3, alpha.re);
+      t = z64{(beta - alpha.re) / beta, -alpha.im / beta};
+      // 1/(alpha - beta)
+      double dr = alpha.re - beta, di = alpha.im;
+      double den = dr * dr + di * di;
+      sc = z64{dr / den, -di / den};
+    }
+    ee[b * sd + i] = beta;
+    tau[b * sd + i] = t;
+    scal[b * 4 + 0] = sc;
+    scal[b * 4 + 1] = t;
+    s_scale = sc;
+    s_skip = skip;
+  }
+  __syncthreads();
+  const C<R> scR = cfrom64<R>(s_scale);
+  if (!s_skip) {
+    for (int r = i + 2 + threadIdx.x; r < n; r += blockDim.x) A[r + lda * i] = cmul(A[r + lda * i], scR);
+  }
+  if (threadIdx.x == 0) A[(i + 1) + lda * i] = cfrom64<R>(1.0, 0.0);
+}
+
+// P[chunk][r] = sum_{c in chunk} A(r,c) v(c), r,c in [i+1, n), v = A(i+1:n, i).
+template <class R>
+__global__ void __launch_bounds__(HV_RB) k_hemv(const C<R> *Ab, int64_t lda, int64_t sA, const int *nvec, int i,
+                                                C<R> *Pb, int64_t sP, int64_t ldp) {
+  __shared__ C<R> sv[HV_CC];
+  const int b = blockIdx.z;
+  const int n = nvec[b];
+  const int r0 = i + 1;
+  const int c0 = r0 + blockIdx.y * HV_CC;
+  if (r0 >= n || c0 >= n) return;
+  const C<R> *A = Ab + b * sA;
+  for (int t = threadIdx.x; t < HV_CC; t += blockDim.x) {
+    int c = c0 + t;
+    sv[t] = (c < n) ? A[c + lda * i] : cz<R>();
+  }
+  __syncthreads();
+  const int r = r0 + blockIdx.x * HV_RB + threadIdx.x;
+  if (r >= n) return;
+  const int cend = min(HV_CC, n - c0);
+  C<R> acc = cz<R>();
+  const C<R> *Ar = A + r + lda * c0;
+  int t = 0;
+  for (; t + 4 <= cend; t += 4) {
+    C<R> a0 = Ar[lda * (t + 0)], a1 = Ar[lda * (t + 1)], a2 = Ar[lda * (t + 2)], a3 = Ar[lda * (t + 3)];
+    cmac(acc, a0, sv[t + 0]);
+    cmac(acc, a1, sv[t + 1]);
+    cmac(acc, a2, sv[t + 2]);
+    cmac(acc, a3, sv[t + 3]);
+  }
+  for (; t < cend; ++t) cmac(acc, Ar[lda * t], sv[t]);
+  Pb[b * sP + (int64_t)blockIdx.y * ldp + r] = cfin(acc);
+}
+
+// X[c] = V(:,c)^H v (c < jj), X[jj+c] = W(:,c)^H v, over rows [i+1, n).
+template <class R>
+__global__ void __launch_bounds__(TR_NT) k_dots(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Wb, int64_t sW,
+                                                const int *nvec, int i, int k0, int jj, z64 *X, int ldx) {
+  __shared__ double red[32];
+  const int b = blockIdx.y;
+  const int n = nvec[b];
+  if (i >= n - 1) return;
+  const C<R> *A = Ab + b * sA;
+  const C<R> *W = Wb + b * sW;
+  const int c2 = blockIdx.x;
+  const bool useW = c2 >= jj;
+  const int c = useW ? c2 - jj : c2;
+  const C<R> *Xc = useW ? (W + lda * c) : (A + lda * (k0 + c));
+  C<R> acc = cz<R>();
+  for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) cmacc(acc, Xc[r], A[r + lda * i]);
+  z64 s = block_sum_z<TR_NT>(cto64(cfin(acc)), red);
+  if (threadIdx.x == 0) X[b * ldx + c2] = s;
+}
+
+// w = tau (y - W x1 - V x2) with y = sum of hemv partials; partial w^H v.
+template <class R>
+__global__ void __launch_bounds__(TR_NT) k_wcorr(const C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
+                                                 const C<R> *Pb, int64_t sP, int64_t ldp, const int *nvec, int i,
+                                                 int k0, int jj, const z64 *X, int ldx, const z64 *scal, z64 *wv,
+                                                 int nrb) {
+  __shared__ C<R> x1[64], x2[64];
+  __shared__ double red[32];
+  const int b = blockIdx.y;
+  const int n = nvec[b];
+  if (i >= n - 1) return;
+  const C<R> *A = Ab + b * sA;
+  C<R> *W = Wb + b * sW;
+  for (int c = threadIdx.x; c < jj; c += blockDim.x) {
+    x1[c] = cfrom64<R>(X[b * ldx + c]);       // V^H v
+    x2[c] = cfrom64<R>(X[b * ldx + jj + c]);  // W^H v
+  }
+  __syncthreads();
+  const int r = i + 1 + blockIdx.x * TR_NT + threadIdx.x;
+  z64 part{0.0, 0.0};
+  if (r < n) {
+    const int nch = cdiv_dev(n - i - 1, HV_CC);
+    C<R> y = cz<R>();
+    for (int ch = 0; ch < nch; ++ch) y = cadd(y, Pb[b * sP + (int64_t)ch * ldp + r]);
+    if (jj > 0) {
+      C<R> acc = cz<R>();
+      for (int c = 0; c < jj; ++c) {
+        cmac(acc, W[r + lda * c], x1[c]);
+        cmac(acc, A[r + lda * (k0 + c)], x2[c]);
+      }
+      y = csub(y, cfin(acc));
+    }
+    const C<R> t = cfrom64<R>(scal[b * 4 + 1]);
+    C<R> w = cmul(t, y);
+    W[r + lda * jj] = w;
+    z64 w64 = cto64(w), v64 = cto64(A[r + lda * i]);
+    part = z64{w64.re * v64.re + w64.im * v64.im, w64.re * v64.im - w64.im * v64.re};
+  }
+  z64 s = block_sum_z<TR_NT>(part, red);
+  if (threadIdx.x == 0) wv[b * nrb + blockIdx.x] = s;
+}
+
+// alpha = -1/2 tau (w^H v) ; w += alpha v
+template <class R>
+__global__ void __launch_bounds__(TR_NT) k_wfin(const C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
+                                                const int *nvec, int i, int jj, int nparts, const z64 *scal,
+                                                const z64 *wv, int nrb) {
+  __shared__ z64 s_alpha;
+  const int b = blockIdx.y;
+  const int n = nvec[b];
+  if (i >= n - 1) return;
+  if (threadIdx.x == 0) {
+    z64 s{0.0, 0.0};
+    for (int k = 0; k < nparts; ++k) {
+      s.re += wv[b * nrb + k].re;
+      s.im += wv[b * nrb + k].im;
+    }
+    z64 t = scal[b * 4 + 1];
+    z64 ts = zmul(t, s);
+    s_alpha = z64{-0.5 * ts.re, -0.5 * ts.im};
+  }
+  __syncthreads();
+  const int r = i + 1 + blockIdx.x * TR_NT + threadIdx.x;
+  if (r >= n) return;
+  const C<R> *A = Ab + b * sA;
+  C<R> *W = Wb + b * sW;
+  C<R> acc = W[r + lda * jj];
+  cmac(acc, cfrom64<R>(s_alpha), A[r + lda * i]);
+  W[r + lda * jj] = cfin(acc);
+}
+
+// Trailing update A(k1:n, k1:n) -= V W^H + W V^H (full square), K = jb.
+constexpr int HK_T = 64, HK_K = 8;
+template <class R>
+__global__ void __launch_bounds__(256) k_her2k(C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Wb, int64_t sW,
+                                               const int *nvec, int k0, int jb) {
+  __shared__ C<R> sVr[HK_K][HK_T], sWr[HK_K][HK_T], sVc[HK_K][HK_T], sWc[HK_K][HK_T];
+  const int b = blockIdx.z;
+  const int n = nvec[b];
+  const int k1 = k0 + jb;
+  const int r0 = k1 + blockIdx.x * HK_T, c0 = k1 + blockIdx.y * HK_T;
+  if (r0 >= n || c0 >= n) return;
+  C<R> *A = Ab + b * sA;
+  const C<R> *W = Wb + b * sW;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  C<R> acc[4][4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = cz<R>();
+  const int jmax = min(jb, n - 1 - k0);  // reflectors that exist in this matrix
+  for (int kc = 0; kc < jmax; kc += HK_K) {
+    for (int e = threadIdx.x; e < HK_K * HK_T; e += 256) {
+      int x = e % HK_T, y = e / HK_T;
+      int k = kc + y;
+      int rr = r0 + x, cc = c0 + x;
+      bool ok = k < jmax;
+      sVr[y][x] = (ok && rr < n) ? A[rr + lda * (k0 + k)] : cz<R>();
+      sWr[y][x] = (ok && rr < n) ? W[rr + lda * k] : cz<R>();
+      sVc[y][x] = (ok && cc < n) ? cconj(A[cc + lda * (k0 + k)]) : cz<R>();
+      sWc[y][x] = (ok && cc < n) ? cconj(W[cc + lda * k]) : cz<R>();
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int k = 0; k < HK_K; ++k) {
+      C<R> vr[4], wr[4], vc[4], wc[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        vr[p] = sVr[k][tx + 16 * p];
+        wr[p] = sWr[k][tx + 16 * p];
+        vc[p] = sVc[k][ty + 16 * p];
+        wc[p] = sWc[k][ty + 16 * p];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          cmac(acc[p][q], vr[p], wc[q]);
+          cmac(acc[p][q], wr[p], vc[q]);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int rr = r0 + tx + 16 * p, cc = c0 + ty + 16 * q;
+      if (rr < n && cc < n) {
+        C<R> *x = &A[rr + lda * cc];
+        *x = csub(*x, cfin(acc[p][q]));
+      }
+    }
+}
+
+template <class R>
+cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
+  C<R> *A = (C<R> *)w.A;
+  C<R> *W = (C<R> *)w.W;
+  C<R> *P = (C<R> *)w.P;
+  const int B = w.B, nmax = w.nmax, nb = w.nb;
+  const int64_t lda = w.lda, sA = w.sA, sW = (int64_t)w.lda * nb, sP = (int64_t)w.nchunk * w.lda;
+  const int64_t sd = w.nmax;
+  for (int k0 = 0; k0 < nmax; k0 += nb) {
+    const int jb = min(nb, nmax - k0);
+    for (int jj = 0; jj < jb; ++jj) {
+      const int i = k0 + jj;
+      const int nparts = cdiv(nmax - i, TR_NT);
+      k_colupd<R><<<dim3(nparts, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, w.d, sd, w.nrm, w.nrb);
+      if (i >= nmax - 1) {
+        count_launch(1);
+        continue;
+      }
+      k_reflector<R><<<B, TR_NT, 0, s>>>(A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal);
+      const int m = nmax - i - 1;
+      dim3 gh(cdiv(m, HV_RB), cdiv(m, HV_CC), B);
+      k_hemv<R><<<gh, HV_RB, 0, s>>>(A, lda, sA, w.nvec, i, P, sP, lda);
+      if (jj > 0) k_dots<R><<<dim3(2 * jj, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb);
+      const int nr = cdiv(m, TR_NT);
+      k_wcorr<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, P, sP, lda, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb,
+                                               w.scal, (z64 *)w.wv, w.nrb);
+      k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nr, w.scal, (z64 *)w.wv, w.nrb);
+      count_launch(jj > 0 ? 6 : 5);
+    }
+    const int k1 = k0 + jb;
+    if (k1 < nmax) {
+      const int m = nmax - k1;
+      dim3 g(cdiv(m, HK_T), cdiv(m, HK_T), B);
+      k_her2k<R><<<g, 256, 0, s>>>(A, lda, sA, W, sW, w.nvec, k0, jb);
+      count_launch(1);
+    }
+  }
+  return cudaGetLastError();
+}
+
+// ===========================================================================
+// Stage 2: eigenvalues of the tridiagonal matrix (FP64 bisection)
+// ===========================================================================
+__device__ __forceinline__ int sturm_count(const double *d, const double *e2, int n, double x, double pivmin) {
+  double q = d[0] - x;
+  if (fabs(q) <= pivmin) q = -pivmin;
+  int c = q < 0.0;
+  for (int k = 1; k < n; ++k) {
+    q = d[k] - e2[k - 1] / q - x;
+    if (fabs(q) <= pivmin) q = -pivmin;
+    c += q < 0.0;
+  }
+  return c;
+}
+
+// Gerschgorin interval, pivmin and the index range of the wanted eigenvalues.
+__global__ void k_tdprep(const double *dd, const double *ee, int64_t sd, const int *nvec, char range, double vl,
+                         double vu, int64_t il, int64_t iu, int64_t *rng, double *tinfo, int64_t *info) {
+  const int b = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const int n = nvec[b];
+  const double *d = dd + b * sd;
+  const double *e = ee + b * sd;
+  double gl = d[0], gu = d[0], emax2 = 0.0;
+  for (int k = 0; k < n; ++k) {
+    double off = (k > 0 ? fabs(e[k - 1]) : 0.0) + (k < n - 1 ? fabs(e[k]) : 0.0);
+    gl = fmin(gl, d[k] - off);
+    gu = fmax(gu, d[k] + off);
+    if (k < n - 1) emax2 = fmax(emax2, e[k] * e[k]);
+  }
+  const double ulp = DBL_EPSILON;
+  const double safmin = DBL_MIN;
+  double tnorm = fmax(fabs(gl), fabs(gu));
+  double pivmin = safmin * fmax(1.0, emax2);
+  const double fudge = 2.1;
+  gl = gl - fudge * tnorm * ulp * n - fudge * 2.0 * pivmin;
+  gu = gu + fudge * tnorm * ulp * n + fudge * 2.0 * pivmin;
+  int64_t lo = 1, hi = n;
+  if (range == 'I') {
+    lo = il;
+    hi = iu;
+  } else if (range == 'V') {
+    // eigenvalues in the half-open interval (vl, vu]
+    // local e^2 recomputed on the fly
+    double q;
+    int cl = 0, cu = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+      double x = pass == 0 ? vl : vu;
+      q = d[0] - x;
+      if (fabs(q) <= pivmin) q = -pivmin;
+      int c = q < 0.0;
+      for (int k = 1; k < n; ++k) {
+        q = d[k] - (e[k - 1] * e[k - 1]) / q - x;
+        if (fabs(q) <= pivmin) q = -pivmin;
+        c += q < 0.0;
+      }
+      if (pass == 0)
+        cl = c;
+      else
+        cu = c;
+    }
+    lo = cl + 1;
+    hi = cu;
+  }
+  int64_t m = hi - lo + 1;
+  if (m < 0) m = 0;
+  rng[b * 8 + 0] = lo;
+  rng[b * 8 + 1] = hi;
+  rng[b * 8 + 2] = m;
+  tinfo[b * 8 + 0] = gl;
+  tinfo[b * 8 + 1] = gu;
+  tinfo[b * 8 + 2] = tnorm;
+  tinfo[b * 8 + 3] = pivmin;
+  info[b] = 0;
+}
+
+__global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *ee, int64_t sd, const int *nvec,
+                                                const int64_t *rng, const double *tinfo, double abstol, double *wout,
+                                                int64_t *info, int use_smem) {
+  extern __shared__ double sm[];
+  const int b = blockIdx.y;
+  const int n = nvec[b];
+  const double *d = dd + b * sd;
+  const double *e = ee + b * sd;
+  double *sd_ = sm;
+  double *se2 = sm + n;
+  if (use_smem) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      sd_[k] = d[k];
+      se2[k] = (k < n - 1) ? e[k] * e[k] : 0.0;
+    }
+    __syncthreads();
+  }
+  const int64_t lo_idx = rng[b * 8 + 0];
+  const int64_t m = rng[b * 8 + 2];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const int64_t idx = lo_idx + j;
+  const double pivmin = tinfo[b * 8 + 3];
+  double lo = tinfo[b * 8 + 0], hi = tinfo[b * 8 + 1];
+  const double ulp = DBL_EPSILON;
+  bool conv = false;
+  for (int it = 0; it < 256; ++it) {
+    double tol = fmax(fmax(abstol, pivmin), 2.0 * ulp * fmax(fabs(lo), fabs(hi)));
+    if (hi - lo <= tol) {
+      conv = true;
+      break;
+    }
+    double mid = 0.5 * (lo + hi);
+    int c;
+    if (use_smem)
+      c = sturm_count(sd_, se2, n, mid, pivmin);
+    else {
+      double q = d[0] - mid;
+      if (fabs(q) <= pivmin) q = -pivmin;
+      c = q < 0.0;
+      for (int k = 1; k < n; ++k) {
+        q = d[k] - (e[k - 1] * e[k - 1]) / q - mid;
+        if (fabs(q) <= pivmin) q = -pivmin;
+        c += q < 0.0;
+      }
+    }
+    if (c >= idx)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  if (!conv) atomicOr((unsigned long long *)&info[b], (unsigned long long)PP_INFO_NOCONV);
+  wout[b * sd + j] = 0.5 * (lo + hi);
+}
+
+cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, int64_t il, int64_t iu, double abstol,
+                                cudaStream_t s) {
+  const int64_t sd = w.nmax;
+  k_tdprep<<<w.B, 32, 0, s>>>(w.d, w.e, sd, w.nvec, range, vl, vu, il, iu, w.rng, w.tinfo, w.info);
+  size_t smem = 2 * (size_t)w.nmax * sizeof(double);
+  int use_smem = smem <= 200 * 1024;
+  if (use_smem) {
+    PP_CUDA_TRY(cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  } else {
+    smem = 0;
+  }
+  dim3 g(cdiv(w.nmax, 128), w.B);
+  k_bisect<<<g, 128, smem, s>>>(w.d, w.e, sd, w.nvec, w.rng, w.tinfo, abstol, w.w, w.info, use_smem);
+  count_launch(2);
+  return cudaGetLastError();
+}
+
+
+// ===========================================================================
+// Stage 3: eigenvectors of T by inverse iteration
+// ===========================================================================
+__global__ void k_clusters(const double *ww, int64_t sd, const int64_t *rng, const double *tinfo, int *cls,
+                           int64_t scl, int *ncl) {
+  const int b = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const int64_t m = rng[b * 8 + 2];
+  const double tnorm = tinfo[b * 8 + 2];
+  const double ortol = 1e-7 * tnorm;
+  const double *w = ww + b * sd;
+  int c = 0;
+  for (int64_t j = 0; j < m; ++j) {
+    if (j == 0 || w[j] - w[j - 1] > ortol) cls[b * scl + c++] = (int)j;
+  }
+  cls[b * scl + c] = (int)m;
+  ncl[b] = c;
+}
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
+// One thread per cluster of eigenvalues (clusters cbase .. cbase+T-1).
+// LU of T - lam I with partial pivoting: row k of U holds (u0,u1,u2) at
+// columns (k, k+1, k+2); l is the multiplier, piv marks a row interchange.
+// Scratch is interleaved by thread ([row][field][thread]) for coalescing.
+template <class R>
+__global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee, int64_t sd, const int *nvec,
+                                              const double *ww, const int64_t *rng, const double *tinfo,
+                                              const int *cls, int64_t scl, const int *ncl, int cbase, C<R> *Eb,
+                                              int64_t lde, int64_t sE, double *scratch, uint8_t *pivb, int64_t T,
+                                              int64_t sS, int64_t sPv, int64_t *info) {
+  const int b = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = cbase + t;
+  if (t >= T || c >= ncl[b]) return;
+  const int n = nvec[b];
+  const double *d = dd + b * sd;
+  const double *e = ee + b * sd;
+  const double *w = ww + b * sd;
+  C<R> *E = Eb + b * sE;
+  double *S = scratch + b * sS;
+  uint8_t *PV = pivb + b * sPv;
+#define SU0(k) S[((int64_t)(k)*4 + 0) * T + t]
+#define SU1(k) S[((int64_t)(k)*4 + 1) * T + t]
+#define SU2(k) S[((int64_t)(k)*4 + 2) * T + t]
+#define SL(k) S[((int64_t)(k)*4 + 3) * T + t]
+#define PIV(k) PV[(int64_t)(k)*T + t]
+#define XV(k) E[(k) + lde * j].re
+  const double tnorm = tinfo[b * 8 + 2];
+  const double eps = DBL_EPSILON * 0.5;
+  const double pivtol = fmax(eps * tnorm, DBL_MIN);
+  const int j0 = cls[b * scl + c], j1 = cls[b * scl + c + 1];
+  double lam_prev = 0.0;
+  int bad = 0;
+  for (int j = j0; j < j1; ++j) {
+    double lam = w[j];
+    if (j > j0) {
+      const double pert = 10.0 * eps * fmax(fabs(lam), 1e-3 * tnorm);
+      if (lam <= lam_prev + pert) lam = lam_prev + pert;
+    }
+    lam_prev = lam;
+    // ---- factor T - lam I
+    double p = d[0] - lam, qv = (n > 1) ? e[0] : 0.0;
+    for (int k = 0; k < n - 1; ++k) {
+      const double ck = e[k];
+      const double ak1 = d[k + 1] - lam;
+      const double bk1 = (k + 1 < n - 1) ? e[k + 1] : 0.0;
+      double u0, u1, u2, l, pn, qn;
+      uint8_t sw;
+      if (fabs(p) >= fabs(ck)) {
+        l = (p == 0.0) ? 0.0 : ck / p;
+        u0 = p;
+        u1 = qv;
+        u2 = 0.0;
+        pn = ak1 - l * qv;
+        qn = bk1;
+        sw = 0;
+      } else {
+        l = p / ck;
+        u0 = ck;
+        u1 = ak1;
+        u2 = bk1;
+        pn = qv - l * ak1;
+        qn = -l * bk1;
+        sw = 1;
+      }
+      SU0(k) = (fabs(u0) < pivtol) ? copysign(pivtol, u0) : u0;
+      SU1(k) = u1;
+      SU2(k) = u2;
+      SL(k) = l;
+      PIV(k) = sw;
+      p = pn;
+      qv = qn;
+    }
+    SU0(n - 1) = (fabs(p) < pivtol) ? copysign(pivtol, p) : p;
+    SU1(n - 1) = 0.0;
+    SU2(n - 1) = 0.0;
+    // ---- deterministic start vector in (-1, 1)
+    const uint32_t seed = hash32((uint32_t)j * 2654435761u ^ (uint32_t)b * 40503u ^ 0x9e3779b9u);
+    for (int k = 0; k < n; ++k) {
+      uint32_t h = hash32(seed + (uint32_t)k * 0x85ebca6bu);
+      double x = ((double)(h >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
+      E[k + lde * j] = cfrom64<R>(x, 0.0);
+    }
+    bool ok = true;
+    for (int it = 0; it < 3 && ok; ++it) {
+      // L solve with the recorded interchanges
+      double xk = RT<R>::to(XV(0));
+      for (int k = 0; k < n - 1; ++k) {
+        const double xk1 = RT<R>::to(XV(k + 1));
+        const double l = SL(k);
+        if (PIV(k)) {
+          XV(k) = RT<R>::from(xk1);
+          xk = xk - l * xk1;
+        } else {
+          XV(k) = RT<R>::from(xk);
+          xk = xk1 - l * xk;
+        }
+      }
+      XV(n - 1) = RT<R>::from(xk);
+      // U solve
+      double y1 = 0.0, y2 = 0.0, amax = 0.0;
+      for (int k = n - 1; k >= 0; --k) {
+        const double y = (RT<R>::to(XV(k)) - SU1(k) * y1 - SU2(k) * y2) / SU0(k);
+        XV(k) = RT<R>::from(y);
+        amax = fmax(amax, fabs(y));
+        y2 = y1;
+        y1 = y;
+      }
+      if (!(amax > 0.0) || !isfinite(amax)) {
+        ok = false;
+        break;
+      }
+      const double inv = 1.0 / amax;
+      for (int k = 0; k < n; ++k) XV(k) = RT<R>::from(RT<R>::to(XV(k)) * inv);
+      // modified Gram-Schmidt against the earlier members of the cluster
+      for (int pass = 0; pass < 2 && j > j0; ++pass) {
+        for (int jp = j0; jp < j; ++jp) {
+          double dot = 0.0;
+          for (int k = 0; k < n; ++k) dot += RT<R>::to(E[k + lde * jp].re) * RT<R>::to(XV(k));
+          for (int k = 0; k < n; ++k) XV(k) = RT<R>::from(RT<R>::to(XV(k)) - dot * RT<R>::to(E[k + lde * jp].re));
+        }
+      }
+      double nrm2 = 0.0;
+      for (int k = 0; k < n; ++k) {
+        const double v = RT<R>::to(XV(k));
+        nrm2 += v * v;
+      }
+      if (!(nrm2 > 1e-280)) {
+        ok = false;
+        break;
+      }
+      const double sc = 1.0 / sqrt(nrm2);
+      for (int k = 0; k < n; ++k) XV(k) = RT<R>::from(RT<R>::to(XV(k)) * sc);
+    }
+    if (!ok) bad = 1;
+    // sign convention of dstein: the largest component is positive
+    double big = -1.0;
+    int kb = 0;
+    for (int k = 0; k < n; ++k) {
+      const double v = fabs(RT<R>::to(XV(k)));
+      if (v > big) {
+        big = v;
+        kb = k;
+      }
+    }
+    const double sgn = RT<R>::to(XV(kb)) < 0.0 ? -1.0 : 1.0;
+    for (int k = 0; k < n; ++k) E[k + lde * j] = cfrom64<R>(RT<R>::to(XV(k)) * sgn, 0.0);
+  }
+  if (bad) atomicOr((unsigned long long *)&info[b], (unsigned long long)PP_INFO_NOORTH);
+#undef SU0
+#undef SU1
+#undef SU2
+#undef SL
+#undef PIV
+#undef XV
+}
+
+template <class R>
+cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
+  const int64_t sd = w.nmax;
+  const int64_t scl = w.nmax + 1;
+  k_clusters<<<w.B, 32, 0, s>>>(w.w, sd, w.rng, w.tinfo, w.cls, scl, w.ncl);
+  count_launch(1);
+  const int64_t T = w.scratch_threads;
+  const int64_t sS = (int64_t)4 * w.nmax * T;
+  const int64_t sPv = (int64_t)w.nmax * T;
+  for (int64_t cb = 0; cb < w.mcap; cb += T) {
+    dim3 g(cdiv(T, 64), w.B);
+    k_invit<R><<<g, 64, 0, s>>>(w.d, w.e, sd, w.nvec, w.w, w.rng, w.tinfo, w.cls, scl, w.ncl, (int)cb, (C<R> *)w.E,
+                                w.lde, w.sE, w.scratch, w.piv, T, sS, sPv, w.info);
+    count_launch(1);
+  }
+  return cudaGetLastError();
+}
+
+// ===========================================================================
+// Stage 4: back-transform E = Q Z
+// ===========================================================================
+constexpr int BT_J = 64;     // columns per block
+constexpr int BT_RK = 16;    // rows per k-step
+constexpr int BT_RCH = 512;  // rows per split-K chunk
+
+// Wp[ks][a][j] = sum_{r in chunk ks} conj(V(r,a)) X(r,j) for a < jb.
+// V(r,a) = A(r, k0+a) for r >= k0+a+1 (zero above).  X is E (ncol = m of
+// the matrix) or, with x_is_v, the panel V itself (ncol = jb, same mask).
+template <class R>
+__global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Xb, int64_t ldx,
+                                             int64_t sX, int x_is_v, const int *nvec, const int64_t *rng, int k0,
+                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp) {
+  __shared__ C<R> sV[BT_RK][32];
+  __shared__ C<R> sXt[BT_RK][BT_J];
+  const int b = blockIdx.z;
+  const int n = nvec[b];
+  const int ncol = x_is_v ? jb : (int)rng[b * 8 + 2];
+  const int j0 = blockIdx.x * BT_J;
+  const int ks = blockIdx.y;
+  const int rbeg = k0 + 1 + ks * BT_RCH;
+  if (j0 >= ncol || rbeg >= n) return;
+  const C<R> *A = Ab + b * sA;
+  const C<R> *X = x_is_v ? (A + lda * k0) : (Xb + b * sX);
+  const int64_t ldX = x_is_v ? lda : ldx;
+  const int tj = threadIdx.x & 63, ta = threadIdx.x >> 6;
+  C<R> acc[8];
+#pragma unroll
+  for (int p = 0; p < 8; ++p) acc[p] = cz<R>();
+  const int rend = min(n, rbeg + BT_RCH);
+  for (int r0 = rbeg; r0 < rend; r0 += BT_RK) {
+    for (int e = threadIdx.x; e < BT_RK * 32; e += 256) {
+      const int a = e & 31, rr = e >> 5;
+      const int r = r0 + rr;
+      sV[rr][a] = (a < jb && r < rend && r >= k0 + a + 1) ? cconj(A[r + lda * (k0 + a)]) : cz<R>();
+    }
+    for (int e = threadIdx.x; e < BT_RK * BT_J; e += 256) {
+      const int jx = e & 63, rr = e >> 6;
+      const int r = r0 + rr, j = j0 + jx;
+      bool ok = r < rend && j < ncol;
+      if (x_is_v) ok = ok && r >= k0 + j + 1;
+      sXt[rr][jx] = ok ? X[r + ldX * j] : cz<R>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < BT_RK; ++rr) {
+      const C<R> xv = sXt[rr][tj];
+#pragma unroll
+      for (int p = 0; p < 8; ++p) cmac(acc[p], sV[rr][ta + 4 * p], xv);
+    }
+    __syncthreads();
+  }
+  const int j = j0 + tj;
+  if (j < ncol) {
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+      const int a = ta + 4 * p;
+      if (a < jb) Wp[b * sWp + ((int64_t)ks * 32 + a) * ldwp + j] = cfin(acc[p]);
+    }
+  }
+}
+
+// Sum the split-K partials.  mode 0: G = V^H V (z64, 32x32).  mode 1:
+// Y = Tf * (V^H E), Tf upper triangular, written to Wb.
+template <class R>
+__global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int64_t sWp, const int *nvec,
+                                              const int64_t *rng, int k0, int jb, int mode, z64 *G, const z64 *Tf,
+                                              C<R> *Wb, int64_t sWb) {
+  __shared__ C<R> col[32][64];
+  __shared__ z64 sT[32][32];
+  const int b = blockIdx.y;
+  const int n = nvec[b];
+  const int ncol = mode == 0 ? jb : (int)rng[b * 8 + 2];
+  const int nks = (n - k0 - 1 + BT_RCH - 1) / BT_RCH;
+  if (mode == 1) {
+    for (int e = threadIdx.x; e < 32 * 32; e += 64) sT[e / 32][e % 32] = Tf[b * 1024 + e];
+  }
+  __syncthreads();
+  const int j = blockIdx.x * 64 + threadIdx.x;
+  if (j >= ncol || nks <= 0) return;
+  for (int a = 0; a < jb; ++a) {
+    C<R> s = cz<R>();
+    for (int ks = 0; ks < nks; ++ks) s = cadd(s, Wp[b * sWp + ((int64_t)ks * 32 + a) * ldwp + j]);
+    col[a][threadIdx.x] = s;
+  }
+  if (mode == 0) {
+    for (int a = 0; a < jb; ++a) G[b * 1024 + a * 32 + j] = cto64(col[a][threadIdx.x]);
+    return;
+  }
+  for (int a = 0; a < jb; ++a) {
+    C<R> acc = cz<R>();
+    for (int a2 = a; a2 < jb; ++a2) cmac(acc, cfrom64<R>(sT[a][a2]), col[a2][threadIdx.x]);
+    Wb[b * sWb + (int64_t)a * ldwp + j] = cfin(acc);
+  }
+}
+
+// Tf (zlarft, forward, columnwise): Tf(a,a) = tau_a,
+// Tf(0:a, a) = -tau_a Tf(0:a, 0:a) G(0:a, a).
+__global__ void k_buildT(const z64 *G, const z64 *tau, int64_t sd, const int *nvec, int k0, int jb, z64 *Tf) {
+  __shared__ z64 sT[32][32];
+  __shared__ z64 tmp[32];
+  const int b = blockIdx.x;
+  const int n = nvec[b];
+  const int a = threadIdx.x;
+  for (int e = a; e < 1024; e += 32) sT[e / 32][e % 32] = z64{0.0, 0.0};
+  __syncthreads();
+  for (int jj = 0; jj < jb; ++jj) {
+    const int i = k0 + jj;
+    const z64 tj = (i < n - 1) ? tau[b * sd + i] : z64{0.0, 0.0};
+    if (a < jj) {
+      z64 acc{0.0, 0.0};
+      for (int a2 = a; a2 < jj; ++a2) {
+        const z64 g = G[b * 1024 + a2 * 32 + jj];
+        const z64 tt = sT[a][a2];
+        acc.re += tt.re * g.re - tt.im * g.im;
+        acc.im += tt.re * g.im + tt.im * g.re;
+      }
+      tmp[a] = acc;
+    }
+    __syncthreads();
+    if (a < jj) {
+      const z64 v = zmul(tj, tmp[a]);
+      sT[a][jj] = z64{-v.re, -v.im};
+    }
+    if (a == jj) sT[jj][jj] = tj;
+    __syncthreads();
+  }
+  for (int e = a; e < 1024; e += 32) Tf[b * 1024 + e] = sT[e / 32][e % 32];
+}
+
+// E(r, j) -= sum_a V(r, a) Y(a, j), r in [k0+1, n), j < m.
+constexpr int AV_T = 64, AV_K = 16;
+template <class R>
+__global__ void __launch_bounds__(256) k_applyV(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Wb,
+                                                int64_t ldwp, int64_t sWb, C<R> *Eb, int64_t lde, int64_t sE,
+                                                const int *nvec, const int64_t *rng, int k0, int jb) {
+  __shared__ C<R> sV[AV_K][AV_T];
+  __shared__ C<R> sY[AV_K][AV_T];
+  const int b = blockIdx.z;
+  const int n = nvec[b];
+  const int m = (int)rng[b * 8 + 2];
+  const int r0 = k0 + 1 + blockIdx.x * AV_T, c0 = blockIdx.y * AV_T;
+  if (r0 >= n || c0 >= m) return;
+  const C<R> *A = Ab + b * sA;
+  const C<R> *Y = Wb + b * sWb;
+  C<R> *E = Eb + b * sE;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  C<R> acc[4][4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = cz<R>();
+  for (int kc = 0; kc < jb; kc += AV_K) {
+    for (int e = threadIdx.x; e < AV_K * AV_T; e += 256) {
+      const int x = e % AV_T, y = e / AV_T;
+      const int a = kc + y;
+      const int r = r0 + x, c = c0 + x;
+      sV[y][x] = (a < jb && r < n && r >= k0 + a + 1) ? A[r + lda * (k0 + a)] : cz<R>();
+      sY[y][x] = (a < jb && c < m) ? Y[(int64_t)a * ldwp + c] : cz<R>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < AV_K; ++k) {
+      C<R> v[4], y[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        v[p] = sV[k][tx + 16 * p];
+        y[p] = sY[k][ty + 16 * p];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cmac(acc[p][q], v[p], y[q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = r0 + tx + 16 * p, c = c0 + ty + 16 * q;
+      if (r < n && c < m) {
+        C<R> *x = &E[r + lde * c];
+        *x = csub(*x, cfin(acc[p][q]));
+      }
+    }
+}
+
+template <class R>
+cudaError_t back_transform(EigWork &w, cudaStream_t s) {
+  const int B = w.B, nmax = w.nmax, nb = w.nb;
+  if (nmax < 2) return cudaSuccess;
+  const int nref = nmax - 1;  // reflector columns 0 .. nmax-2
+  const int64_t ldwp = w.ldwp;
+  const int64_t sWp = (int64_t)w.ksplit * 32 * ldwp;
+  const int64_t sWb = (int64_t)32 * ldwp;
+  const int64_t sd = w.nmax;
+  C<R> *A = (C<R> *)w.A;
+  C<R> *E = (C<R> *)w.E;
+  C<R> *Wp = (C<R> *)w.Wp;
+  C<R> *Wb = (C<R> *)w.Wb;
+  const int kstart = ((nref - 1) / nb) * nb;
+  for (int k0 = kstart; k0 >= 0; k0 -= nb) {
+    const int jb = min(nb, nref - k0);
+    const int ks = cdiv(nmax - k0 - 1, BT_RCH);
+    // Tf from G = V^H V
+    k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, ldwp, sWp);
+    k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb, sWb);
+    k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
+    // Y = Tf V^H E ; E -= V Y
+    k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
+                                                             jb, Wp, ldwp, sWp);
+    k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb);
+    k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
+        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb);
+    count_launch(6);
+  }
+  return cudaGetLastError();
+}
+
+// explicit instantiations
+template cudaError_t tridiagonalize<double>(EigWork &, cudaStream_t);
+template cudaError_t tridiagonalize<df>(EigWork &, cudaStream_t);
+template cudaError_t tridiag_eigenvectors<double>(EigWork &, cudaStream_t);
+template cudaError_t tridiag_eigenvectors<df>(EigWork &, cudaStream_t);
+template cudaError_t back_transform<double>(EigWork &, cudaStream_t);
+template cudaError_t back_transform<df>(EigWork &, cudaStream_t);
+
+}  // namespace pp

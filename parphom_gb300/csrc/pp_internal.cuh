@@ -1,0 +1,119 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "pp_common.cuh"
+
+namespace pp {
+
+// Counts kernel launches made by this library (pp_kernel_launches()).
+void count_launch(int64_t k = 1);
+
+// Per-batch state of the eigensolver.  Every matrix b of a batch of `B`
+// Hermitian matrices has its own order nvec[b] <= nmax; all buffers use the
+// leading dimensions of the largest.  Complex buffers hold 16-byte elements:
+// z64 for the FP64 form, zdf for the double-float form.
+struct EigWork {
+  int B = 0;           // matrices in the batch
+  int nmax = 0;        // largest order
+  int mcap = 0;        // eigenvector columns allocated per matrix
+  int nb = 32;         // panel width
+  int *nvec = nullptr; // [B] device: order of each matrix
+
+  void *A = nullptr;   // [B][nmax*nmax]  D(q), overwritten by the reduction
+  int64_t lda = 0, sA = 0;
+  void *E = nullptr;   // [B][nmax*mcap]  eigenvectors
+  int64_t lde = 0, sE = 0;
+  void *W = nullptr;   // [B][nmax*nb]    zlatrd W panel
+  void *P = nullptr;   // [B][nchunk*nmax] hemv partial sums
+  int nchunk = 0;
+  void *X = nullptr;   // [B][2*nb]       V^H v and W^H v
+  double *nrm = nullptr;  // [B][nrb]     partial column norms
+  z64 *wv = nullptr;      // [B][nrb]     partial w^H v
+  int nrb = 0;            // row blocks for column kernels
+  double *d = nullptr;    // [B][nmax] tridiagonal diagonal
+  double *e = nullptr;    // [B][nmax] off-diagonal (real)
+  z64 *tau = nullptr;     // [B][nmax] reflector scalars
+  z64 *scal = nullptr;    // [B][4]    per-column scalars (scale, tau, alpha)
+
+  // tridiagonal eigen stage
+  double *w = nullptr;    // [B][nmax] eigenvalues (ascending)
+  int64_t *rng = nullptr; // [B][8]  il, iu, m, flags...
+  double *tinfo = nullptr;// [B][8]  gl, gu, tnorm, pivmin
+  int *cls = nullptr;     // [B][nmax+1] cluster starts
+  int *ncl = nullptr;     // [B]
+  double *scratch = nullptr; // inverse-iteration LU factors [B][4*nmax*T]
+  uint8_t *piv = nullptr;    // inverse-iteration pivot flags [B][nmax*T]
+  int64_t scratch_threads = 0;  // T: clusters handled per launch
+  int64_t *info = nullptr;   // [B] info bits
+
+  // back-transform
+  z64 *Tf = nullptr;      // [B][32*32] compact-WY factor of one panel
+  z64 *G = nullptr;       // [B][32*32] Gram matrix V^H V of one panel
+  void *Wb = nullptr;     // [B][32*ldwp]     T V^H E
+  void *Wp = nullptr;     // [B][ksplit][32*ldwp] split-K partials
+  int ksplit = 0;
+  int ldwp = 0;
+
+  size_t bytes = 0;
+};
+
+struct Geometry {
+  int64_t natom = 0, n = 0;
+  double lat[9];       // Fortran lat(i,j) at lat[(i-1)+3*(j-1)]
+  double rec_lat[9];   // 2 pi_f (lat^-1)^T, as lammps_read.F90:228
+  double delta_crys[3][3];  // CD step in reduced coordinates per direction
+  double delta_norm[3];
+  double *d_fc = nullptr;       // n*n Phi, upper triangle mirrored to lower
+  double *d_crys = nullptr;     // natom*3
+  double *d_pos = nullptr;      // natom*3
+  double *d_mass = nullptr;     // natom (mass of each atom)
+  uint16_t *d_mask = nullptr;   // natom*natom image tie sets, (min,max) orientation
+  int64_t nbnd = 0;             // boundary blocks (I<J, non-home image, Phi != 0)
+  int2 *d_bnd = nullptr;        // [nbnd] (I, J)
+  uint16_t *d_bndmask = nullptr;// [nbnd]
+};
+
+// ---- kernels launched from pp_capi.cu -------------------------------------
+cudaError_t geom_build_masks(Geometry &g, cudaStream_t s);
+cudaError_t geom_symmetrize_fc(Geometry &g, int enforce_asr, cudaStream_t s);
+cudaError_t geom_block_nonzero(const Geometry &g, uint8_t *d_flags, cudaStream_t s);
+
+// D(q) for B q-points into 16-byte complex storage (z64 if dfmt==0, zdf if 1).
+cudaError_t assemble_batch(const Geometry &g, const double *d_q, int B, void *A, int64_t lda, int64_t sA,
+                           int dfmt, cudaStream_t s);
+// dD/dq_k (derivative 1..3, method 'A' or 'C') or D (derivative 0), FP64.
+cudaError_t assemble_deriv(const Geometry &g, const double *d_q, int derivative, char method, z64 *out,
+                           int64_t ldo, cudaStream_t s);
+
+// Group velocities: vel[b][3][m] (raw Re e^H dD e), E in 16-byte storage.
+cudaError_t velocities(const Geometry &g, const double *d_q, int B, const void *E, int64_t lde, int64_t sE,
+                       int efmt, const int64_t *d_rng, int mmax, char method, double *d_vraw, double *d_part,
+                       int nsplit, cudaStream_t s);
+
+// Eigen stages, templated on the real type (double / df) in pp_eigen.cu.
+template <class R>
+cudaError_t tridiagonalize(EigWork &w, cudaStream_t s);
+cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, int64_t il, int64_t iu,
+                                double abstol, cudaStream_t s);
+template <class R>
+cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s);
+template <class R>
+cudaError_t back_transform(EigWork &w, cudaStream_t s);
+
+// Output conversion
+cudaError_t finalize_outputs(EigWork &w, int efmt, int raw_lambda, const double *d_vraw, int want_vel, int want_z,
+                             double *w_out, int64_t ldw, double *z_out, int64_t ldz, int64_t zstride, double *vel_out,
+                             int64_t velstride, int64_t *m_out, int64_t *nz_out, int64_t *info_out, int jobz_v,
+                             cudaStream_t s);
+
+}  // namespace pp
+
+#define PP_CUDA_TRY(x)                  \
+  do {                                  \
+    cudaError_t err__ = (x);            \
+    if (err__ != cudaSuccess) return err__; \
+  } while (0)

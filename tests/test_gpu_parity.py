@@ -1,0 +1,134 @@
+"""GPU path (C-ABI library) against the oracle, same inputs."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from parphom_gb300 import api, geometry, synth
+from tests import parity
+
+pytestmark = pytest.mark.gpu
+
+PRECS = [api.PP_PREC_FP64, api.PP_PREC_MIXED]
+
+
+@pytest.fixture(scope="module")
+def tblg28(golden_dir):
+    z = np.load(os.path.join(golden_dir, "tblg21_8_inputs.npz"))
+    S = O.System(z["lat"], z["real_pos"], z["masses"], z["at_types"], z["phi"])
+    ctx = api.PhononContext(z["lat"], S.crys, z["real_pos"], z["masses"], z["at_types"], z["phi"])
+    yield S, ctx, z
+    ctx.close()
+
+
+@pytest.fixture(scope="module")
+def cell148():
+    c = synth.tblg_cell(3)
+    phi = synth.spring_force_constants(c, seed=0)
+    S = O.System.from_cell(c, phi)
+    ctx = api.PhononContext.from_cell(c, phi)
+    yield S, ctx
+    ctx.close()
+
+
+@pytest.mark.parametrize("deriv,method", [(0, "A"), (1, "A"), (2, "A"), (3, "A"), (1, "C"), (2, "C")])
+def test_dynamical_matrix_elements(tblg28, cell148, deriv, method):
+    for S, ctx in ((tblg28[0], tblg28[1]), cell148):
+        for q in ([0.0, 0.0, 0.0], [0.31, -0.12, 0.0], [2 / 3, 1 / 3, 0.0]):
+            Dg = ctx.dynamical_matrix(q, deriv, method)
+            Dr = S.dynmat(q, deriv, method)
+            scale = np.abs(Dr).max()
+            tol = (1e-13 if method == "A" else 1e-7) * scale
+            assert np.abs(Dg - Dr).max() <= tol, (deriv, method, np.abs(Dg - Dr).max() / scale)
+
+
+def _solve_and_check(S, ctx, qs, prec, vel_method="A", rng="A", il=1, iu=1, vl=0.0, vu=0.0, jobz="V", vel=True):
+    opts = api.EigOpts(jobz=jobz, range=rng, il=il, iu=iu, vl=vl, vu=vu, vel=vel, vel_method=vel_method,
+                       precision=prec)
+    res = ctx.solve(qs, opts)
+    n = S.n
+    stats = []
+    for t, q in enumerate(qs):
+        ref = O.solve_q(S, q, jobz=jobz, rng=rng, il=il, iu=iu, vl=vl, vu=vu, vel=vel, vel_method=vel_method)
+        m = len(ref["w_cm"])
+        assert res.m[t] == m
+        assert res.info[t] == 0
+        D = S.dynmat(q)
+        Dn = np.abs(np.linalg.eigvalsh(D)).max()
+        werr = parity.check_frequencies(res.w[t, :m], ref["w_cm"], ref["lam"], n, Dn)
+        st = {"werr": werr}
+        if jobz == "V" or vel:
+            assert res.nz[t] == m
+            Z = res.z[t][:, :m]
+            st["res"], st["orth"] = parity.check_vectors(Z, ref["lam"], D, 1e-11, 1e-10)
+        if vel:
+            vmax = np.abs(ref["vel"]).max()
+            st["vrel"] = parity.check_velocities(res.vel[t, :m], ref["vel"], ref["lam"], Dn, vmax)
+        stats.append(st)
+    return res, stats
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_shipped_cell_bands(tblg28, prec):
+    S, ctx, z = tblg28
+    qs = np.vstack([z["q_symm"], [[0, 0, 0]], z["q_band"][[17, 133, 250]]])
+    _, st = _solve_and_check(S, ctx, qs, prec)
+    print(prec, st)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_synthetic_148_band_path(cell148, prec):
+    S, ctx = cell148
+    qs = synth.band_path(7)
+    _, st = _solve_and_check(S, ctx, qs, prec)
+    print(prec, st)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_central_difference_velocities(cell148, prec):
+    S, ctx = cell148
+    qs = synth.random_qpoints(3, seed=5)
+    _solve_and_check(S, ctx, qs, prec, vel_method="C")
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_range_index(cell148, prec):
+    S, ctx = cell148
+    qs = synth.random_qpoints(2, seed=6)
+    _solve_and_check(S, ctx, qs, prec, rng="I", il=5, iu=60, jobz="N", vel=False)
+    _solve_and_check(S, ctx, qs, prec, rng="I", il=100, iu=180, jobz="V", vel=True)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_range_value(cell148, prec):
+    S, ctx = cell148
+    qs = synth.random_qpoints(2, seed=7)
+    # bounds in the reference's units: they are divided by 15.633302*33.35641
+    # and compared with lambda = omega^2, so lambda in (0.5, 3.0] here
+    _solve_and_check(S, ctx, qs, prec, rng="V", vl=0.5 * O.C_RANGE, vu=3.0 * O.C_RANGE, jobz="V", vel=True)
+    # an empty interval gives m = 0
+    res = ctx.solve(qs[:1], api.EigOpts(range="V", vl=1e-9, vu=2e-9, jobz="N", precision=prec))
+    assert res.m[0] == 0 and res.info[0] == 0
+
+
+def test_eigenvalues_only_many_q(cell148):
+    S, ctx = cell148
+    qs = synth.uniform_grid(4)
+    _solve_and_check(S, ctx, qs, api.PP_PREC_FP64, jobz="N", vel=False)
+
+
+def test_errors(cell148):
+    S, ctx = cell148
+    with pytest.raises(api.PPError) as e:
+        ctx.solve([[0, 0, 0]], api.EigOpts(range="I", il=5, iu=2))
+    assert e.value.code == -5
+    with pytest.raises(api.PPError) as e:
+        ctx.solve([[np.nan, 0, 0]], api.EigOpts())
+    assert e.value.code == 1003
+    c = synth.tblg_cell(3)
+    phi = synth.spring_force_constants(c)
+    phi[0, 5] = np.inf
+    with pytest.raises(api.PPError) as e:
+        api.PhononContext.from_cell(c, phi)
+    assert e.value.code == 1003
