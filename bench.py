@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""Benchmark of the phonon hot path on GB300.
+
+Workload (one "step"): a batch of q-points of the theta = 2.88 deg twisted
+bilayer graphene cell (N = 1588 atoms, 3N = 4764), synthetic spring-model
+force constants (seed 0), q-points on the Gamma-K-M-Gamma path (128 points,
+cycled), frequencies + analytic group velocities (jobz forced to 'V' by the
+velocity switch), mixed-precision form.  `value` is q-points/s with inputs
+resident in HBM; `e2e` the same through the host C-ABI call (q from pinned
+host memory in, frequencies and velocities back to host memory).  Every
+matrix (363 MB per q in double-float complex) is larger than L2, so no L2
+flush is needed between steps.
+
+Also measured: the plain FP64 form on a smaller batch of the same q (the
+ratio the metric names), the largest frequency difference between the two
+forms, per-kernel CUDA-event times for the roofline, SM clocks during the
+timed region, and the CPU oracle on one q (cpu_baseline).
+
+`--impl reference` times the reference-equivalent CPU path (the oracle:
+C restatement of the D(q) assembly + LAPACK zheevx + dense dD/dq velocities)
+on the host cores, one q per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "q-pts/s (w+v_g) at N=1588: mixed/batched vs FP64 GPU at |dw|<1e-4 cm^-1"
+UNIT = "q-pts/s"
+WORKLOAD = "tBLG theta=2.88deg N=1588 (3N=4764), spring FC seed 0, band-path q, w + analytic v_g"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--batch", type=int, default=4, help="q-points per step and rank")
+    p.add_argument("--m", type=int, default=11, help="twist index (11 -> N=1588)")
+    p.add_argument("--fp64-batch", type=int, default=1)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi (profiler runs)")
+    p.add_argument("--roofline-kernels", default="hemv,her2k,vhx,applyV,invit,bisect,vel,assemble")
+    return p.parse_args()
+
+
+def workload(m):
+    from parphom_gb300 import geometry, synth
+    cell = synth.tblg_cell(m)
+    phi = synth.spring_force_constants(cell, seed=0)
+    crys = geometry.crys_from_positions(cell.lat, cell.real_pos)
+    q_all = synth.band_path(128)
+    return cell, phi, crys, q_all
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (the child is always
+    terminated, also on error exit)."""
+
+    def __init__(self, index, enabled=True):
+        self.p = None
+        if not enabled:
+            return
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            import atexit
+            atexit.register(self._kill)
+        except Exception:
+            self.p = None
+
+    def _kill(self):
+        if self.p is not None and self.p.poll() is None:
+            self.p.kill()
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["not sampled"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    """The reference-equivalent CPU path on the host cores, one q per step."""
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    cell, phi, crys, q_all = workload(args.m)
+    S = O.System.from_cell(cell, phi)
+    cores = os.cpu_count()
+    # LAPACK has nothing to warm up: each warm-up step only assembles D(q).
+    for i in range(args.warmup):
+        S.dynmat(q_all[(7 * i + 3) % len(q_all)])
+    # one q-point per timed step; the sample stops early once ~150 s of CPU
+    # time have been spent (one q of this cell takes ~50 s on 16 Grace cores)
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        O.solve_q(S, q_all[(7 * i + 3) % len(q_all)], vel=True, vel_method="A")
+        times.append(time.perf_counter() - t0)
+        if sum(times) > 150.0:
+            break
+    t = sum(times)
+    v = len(times) / t
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
+            "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(times),
+            "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "q_per_step": 1, "l2": "inputs larger than L2"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "1 q-point per step: oracle D(q) (C restatement) + LAPACK zheevx (OpenBLAS, "
+                                       "all host threads) + dense dD/dq velocities"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from parphom_gb300 import api
+
+    cell, phi, crys, q_all = workload(args.m)
+    n = cell.n
+    ctx = api.PhononContext(cell.lat, crys, cell.real_pos, cell.masses, cell.at_types, phi)
+    B = args.batch
+    dev = torch.device("cuda", local)
+    # this rank's q-points: a disjoint slice of the path per rank, cycled
+    q_rank = q_all[rank::world]
+    nbat = max(1, len(q_rank) // B)
+    q_dev = [torch.tensor(np.asfortranarray(np.resize(q_rank[b * B:(b + 1) * B], (B, 3))).ravel(order="F"),
+                          dtype=torch.float64, device=dev) for b in range(nbat)]
+    w_dev = torch.zeros((B, n), dtype=torch.float64, device=dev)
+    v_dev = torch.zeros((B, n, 3), dtype=torch.float64, device=dev)
+    m_dev = torch.zeros(B, dtype=torch.int64, device=dev)
+    nz_dev = torch.zeros_like(m_dev)
+    info_dev = torch.zeros_like(m_dev)
+    opts = api.EigOpts(jobz="N", vel=True, vel_method="A", precision=api.PP_PREC_MIXED)
+    stream = torch.cuda.current_stream()
+
+    def step(i):
+        ctx.solve_device(q_dev[i % nbat], opts, w_dev, m_dev, nz_dev, info_dev, vel_dev=v_dev,
+                         stream=stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    api.kernel_timer(args.roofline_kernels)
+    l0 = api.kernel_launches()
+    clk = Clocks(local, enabled=not args.no_clocks)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        step(args.warmup + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier()
+    launches = api.kernel_launches() - l0
+    ktimes = api.kernel_timer_report()
+    api.kernel_timer("")
+    t = e0.elapsed_time(e1) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    assert int(info_dev.max().item()) == 0 and int(m_dev.min().item()) == n
+    value = world * B * args.steps / t
+
+    extra = {}
+    # plain FP64 form on the same q, and the frequency difference of the two forms
+    if not args.no_fp64:
+        Bf = args.fp64_batch
+        qf = np.resize(q_rank[3:3 + Bf], (Bf, 3))   # off Gamma
+        o64 = api.EigOpts(jobz="N", vel=True, vel_method="A", precision=api.PP_PREC_FP64)
+        omx = api.EigOpts(jobz="N", vel=True, vel_method="A", precision=api.PP_PREC_MIXED)
+        ctx.solve(qf, o64, want_z=False)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r64 = ctx.solve(qf, o64, want_z=False)
+        t64 = time.perf_counter() - t0
+        rmx = ctx.solve(qf, omx, want_z=False)
+        # |w| >= 1 cm^-1 (acoustic modes near Gamma are judged on lambda in the tests)
+        big = np.abs(r64.w) >= 1.0
+        dw = float(np.abs(r64.w - rmx.w)[big].max())
+        vs = max(float(np.abs(r64.vel).max()), 1e-30)
+        dv = float(np.abs(r64.vel - rmx.vel).max() / vs)
+        extra["fp64_form"] = {"value": Bf / t64, "unit": UNIT, "q_per_step": Bf,
+                              "note": "same pipeline, IEEE double in every stage; host API, one step"}
+        extra["mixed_over_fp64"] = None  # filled below from e2e-comparable numbers
+        extra["accuracy"] = {"max_abs_dw_cm1_mixed_vs_fp64": dw, "max_abs_dv_rel_mixed_vs_fp64": dv,
+                             "q_compared": Bf}
+    # end to end through the host C ABI
+    e2e = None
+    if not args.no_e2e:
+        qh = np.resize(q_rank[:B], (B, 3))
+        ctx.solve(qh, opts, want_z=False)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            ctx.solve(np.resize(q_rank[(i * B) % len(q_rank):][:B], (B, 3)), opts, want_z=False)
+        te = time.perf_counter() - t0
+        e2e = {"value": world * B * args.steps / te if world == 1 else B * args.steps / te * world, "unit": UNIT,
+               "h2d_bytes_per_step": 8 * 3 * B, "d2h_bytes_per_step": 8 * B * (n + 3 * n + 3)}
+        if "fp64_form" in extra:
+            extra["mixed_over_fp64"] = e2e["value"] / extra["fp64_form"]["value"]
+    # roofline of the dominant kernel class
+    roof = None
+    if ktimes:
+        dom = max(ktimes, key=lambda k: ktimes[k][1])
+        roof = roofline_for(dom, ktimes[dom], n, B * args.steps)
+        roof["kernel_ms_share"] = {k: round(v[1] / sum(x[1] for x in ktimes.values()), 4) for k, v in ktimes.items()}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(cell, phi, q_all)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "df32x2 (double-float), f64 tridiagonal",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD, "q_per_step_per_gpu": B, "precision": "mixed",
+                           "l2": "inputs larger than L2 (363 MB matrix per q)", "parallelism": f"replicas x{world}"},
+                "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roof,
+                "cpu_baseline": cpu}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def roofline_for(kclass, rec, n, nq):
+    """Algorithmic work of the dominant kernel class over the timed region."""
+    launches, ms = rec
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    src = "of measured" if "hbm_gbs" in peaks else "of fallback"
+    if kclass == "hemv":
+        # each column i reads the trailing (n-i-1)^2 block of 16-byte elements
+        byts = nq * 16.0 * sum((n - i - 1) ** 2 for i in range(n - 1))
+        ach = byts / (ms / 1e3) / 1e9
+        return {"bound": "hbm", "kernel": "k_hemv (double-float Hermitian mat-vec)", "achieved": ach, "peak": hbm,
+                "unit": "GB/s", "frac": ach / hbm, "peak_source": src, "traffic": None,
+                "launches": launches, "avg_launch_ms": ms / launches,
+                "algorithmic_bytes_per_launch": byts / launches}
+    # FP32-pipe kernels (double-float arithmetic): count complex MACs
+    macs = {"her2k": 2.0 * sum((n - k) ** 2 * 32 for k in range(32, n, 32)),
+            "vhx": sum(n * (n - k) * 32.0 for k in range(0, n, 32)),
+            "applyV": sum(n * (n - k) * 32.0 for k in range(0, n, 32))}.get(kclass)
+    if macs is None:
+        return {"bound": "hbm", "kernel": kclass, "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+                "launches": launches, "avg_launch_ms": ms / launches}
+    flops = 8.0 * macs * nq
+    ach = flops / (ms / 1e3) / 1e12
+    return {"bound": "fp32-simt (double-float)", "kernel": kclass, "achieved": ach, "peak": None, "unit": "TFLOP/s",
+            "frac": None, "launches": launches, "avg_launch_ms": ms / launches}
+
+
+def cpu_baseline(cell, phi, q_all):
+    from oracle import oracle as O
+    S = O.System.from_cell(cell, phi)
+    t0 = time.perf_counter()
+    O.solve_q(S, q_all[3], vel=True, vel_method="A")
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "1 q-point of the same workload: oracle D(q) (C restatement) + LAPACK zheevx (OpenBLAS, all "
+                      "host threads) + dense dD/dq velocities"}
+
+
+if __name__ == "__main__":
+    main()

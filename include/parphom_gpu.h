@@ -152,6 +152,13 @@ PP_API int64_t pp_version(void);
  * since load (for launch accounting in benchmarks). */
 PP_API int64_t pp_kernel_launches(void);
 
+/* Instrumentation (no counterpart in the reference): record CUDA events
+ * around every launch of the named kernel classes (comma separated, e.g.
+ * "hemv,vhx,applyV"; NULL or "" disables) and report, one line per class,
+ * "<class> <launches> <total milliseconds>". */
+PP_API int pp_ktimer_enable(const char *names);
+PP_API int pp_ktimer_report(char *buf, int64_t len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,7 +30,7 @@ INFO_NOMEM = 4
 INFO_NOTCOMP = 8
 
 EXPORTED = ("pp_ctx_create", "pp_ctx_destroy", "pp_solve_batch", "pp_solve_batch_device", "pp_dynamical_matrix",
-            "pp_strerror", "pp_version", "pp_kernel_launches")
+            "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report")
 
 _i64 = ctypes.c_int64
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -95,6 +95,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.pp_strerror.restype = ctypes.c_char_p
     L.pp_version.restype = _i64
     L.pp_kernel_launches.restype = _i64
+    L.pp_ktimer_enable.argtypes = [ctypes.c_char_p]
+    L.pp_ktimer_enable.restype = ctypes.c_int
+    L.pp_ktimer_report.argtypes = [ctypes.c_char_p, _i64]
+    L.pp_ktimer_report.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -227,6 +231,45 @@ class PhononContext:
             # per q the buffer holds z[2*(r + n*j)] (column-major) -> numpy (r, j)
             z = np.ascontiguousarray(z.reshape(nq, n, n).transpose(0, 2, 1))
         return Result(m=m, nz=nz, w=w, z=z, vel=vel, info=info)
+
+
+    def solve_device(self, q_dev, opts: EigOpts, w_dev, m_dev, nz_dev, info_dev, vel_dev=None, z_dev=None,
+                     stream: int = 0) -> None:
+        """pp_solve_batch_device: q_dev (nq,3) float64 device tensor in Fortran
+        order (q[t + nq*k]); outputs are device tensors sized like
+        `Result`'s fields (w_dev (nq,n), vel_dev (nq,n,3), z_dev (nq,n,n)
+        complex128, m/nz/info (nq,) int64).  Enqueued on `stream`."""
+        n = self.n
+        nq = int(m_dev.shape[0])
+        rv = PPResultView(ctypes.cast(m_dev.data_ptr(), _ip), ctypes.cast(nz_dev.data_ptr(), _ip),
+                          ctypes.cast(w_dev.data_ptr(), _dp), n,
+                          ctypes.cast(z_dev.data_ptr(), _dp) if z_dev is not None else None, n, 2 * n * n,
+                          ctypes.cast(vel_dev.data_ptr(), _dp) if vel_dev is not None else None, 3 * n, None)
+        oc = opts.to_c()
+        rc = self._lib.pp_solve_batch_device(self._h, ctypes.c_void_p(q_dev.data_ptr()), nq, nq, ctypes.byref(oc),
+                                             ctypes.byref(rv), ctypes.c_void_p(info_dev.data_ptr()),
+                                             ctypes.c_void_p(int(stream)))
+        if rc != 0:
+            raise PPError(rc, "pp_solve_batch_device")
+
+
+def kernel_timer(names: str) -> None:
+    """Record CUDA events around every launch of the named kernel classes
+    (comma separated: hemv, her2k, vhx, applyV, invit, bisect, assemble, vel);
+    empty string disables."""
+    load().pp_ktimer_enable(names.encode())
+
+
+def kernel_timer_report() -> dict:
+    """{kernel class: (launches, total milliseconds)} since the last enable."""
+    L = load()
+    buf = ctypes.create_string_buffer(4096)
+    L.pp_ktimer_report(buf, 4096)
+    out = {}
+    for line in buf.value.decode().splitlines():
+        k, n, ms = line.split()
+        out[k] = (int(n), float(ms))
+    return out
 
 
 def kernel_launches() -> int:

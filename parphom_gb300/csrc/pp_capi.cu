@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <new>
 #include <vector>
 
@@ -15,6 +16,54 @@
 namespace pp {
 static std::atomic<int64_t> g_launches{0};
 void count_launch(int64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+unsigned kt_mask = 0;
+static const char *kt_names[KT_N] = {"assemble", "colupd", "refl", "hemv", "dots", "wcorr", "wfin", "her2k",
+                                     "bisect", "invit", "vhx", "btred", "applyV", "vel"};
+struct KtPending {
+  int k;
+  cudaEvent_t a, b;
+};
+static std::mutex kt_mu;
+static std::vector<KtPending> kt_pending;
+static std::vector<cudaEvent_t> kt_free;
+static cudaEvent_t kt_open[KT_N];
+static int64_t kt_count[KT_N];
+static double kt_ms[KT_N];
+
+static cudaEvent_t kt_event() {
+  if (!kt_free.empty()) {
+    cudaEvent_t e = kt_free.back();
+    kt_free.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+void kt_begin(int k, cudaStream_t s) {
+  std::lock_guard<std::mutex> g(kt_mu);
+  kt_open[k] = kt_event();
+  cudaEventRecord(kt_open[k], s);
+}
+void kt_end(int k, cudaStream_t s) {
+  std::lock_guard<std::mutex> g(kt_mu);
+  cudaEvent_t e = kt_event();
+  cudaEventRecord(e, s);
+  kt_pending.push_back({k, kt_open[k], e});
+}
+static void kt_flush() {
+  for (auto &p : kt_pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      kt_count[p.k] += 1;
+      kt_ms[p.k] += ms;
+    }
+    kt_free.push_back(p.a);
+    kt_free.push_back(p.b);
+  }
+  kt_pending.clear();
+}
 }  // namespace pp
 
 using namespace pp;
@@ -277,6 +326,46 @@ extern "C" {
 int64_t pp_version(void) { return 100; }
 
 int64_t pp_kernel_launches(void) { return pp::g_launches.load(); }
+
+int pp_ktimer_enable(const char *names) {
+  std::lock_guard<std::mutex> g(pp::kt_mu);
+  pp::kt_flush();
+  unsigned mask = 0;
+  if (names) {
+    std::string all(names);
+    size_t p = 0;
+    while (p <= all.size()) {
+      size_t q = all.find(',', p);
+      if (q == std::string::npos) q = all.size();
+      std::string tok = all.substr(p, q - p);
+      for (int k = 0; k < KT_N; ++k)
+        if (tok == pp::kt_names[k]) mask |= 1u << k;
+      p = q + 1;
+    }
+  }
+  for (int k = 0; k < KT_N; ++k) {
+    pp::kt_count[k] = 0;
+    pp::kt_ms[k] = 0.0;
+  }
+  pp::kt_mask = mask;
+  return PP_OK;
+}
+
+int pp_ktimer_report(char *buf, int64_t len) {
+  if (!buf || len <= 0) return -1;
+  std::lock_guard<std::mutex> g(pp::kt_mu);
+  pp::kt_flush();
+  std::string out;
+  char line[128];
+  for (int k = 0; k < KT_N; ++k) {
+    if (!pp::kt_count[k]) continue;
+    snprintf(line, sizeof(line), "%s %lld %.6f\n", pp::kt_names[k], (long long)pp::kt_count[k], pp::kt_ms[k]);
+    out += line;
+  }
+  strncpy(buf, out.c_str(), (size_t)len - 1);
+  buf[len - 1] = 0;
+  return PP_OK;
+}
 
 const char *pp_strerror(int code) {
   switch (code) {

@@ -230,9 +230,9 @@ cudaError_t assemble_batch(const Geometry &g, const double *d_q, int B, void *A,
   GeoDev gd{g.d_fc, g.d_crys, g.d_mass, g.d_mask, g.natom, g.n};
   dim3 grid(cdiv(g.natom, 128), (unsigned)g.natom, B);
   if (dfmt == 0)
-    k_assemble<0><<<grid, 128, 0, s>>>(gd, d_q, A, lda, sA);
+    PP_KT(KT_ASSEMBLE, s, (k_assemble<0><<<grid, 128, 0, s>>>(gd, d_q, A, lda, sA)));
   else
-    k_assemble<1><<<grid, 128, 0, s>>>(gd, d_q, A, lda, sA);
+    PP_KT(KT_ASSEMBLE, s, (k_assemble<1><<<grid, 128, 0, s>>>(gd, d_q, A, lda, sA)));
   count_launch(1);
   return cudaGetLastError();
 }
@@ -462,9 +462,9 @@ cudaError_t velocities(const Geometry &g, const double *d_q, int B, const void *
                                                          va, d_q, method, gtab);
   dim3 grid(cdiv(mmax, 128), nsplit, B);
   if (efmt == 0)
-    k_vel<0><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part);
+    PP_KT(KT_VEL, s, (k_vel<0><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part)));
   else
-    k_vel<1><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part);
+    PP_KT(KT_VEL, s, (k_vel<1><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part)));
   k_vel_reduce<<<dim3(cdiv(mmax, 128), B), 128, 0, s>>>(d_part, nsplit, mstride, d_rng, d_vraw);
   count_launch(3);
   return cudaGetLastError();

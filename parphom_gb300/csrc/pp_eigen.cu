@@ -379,27 +379,27 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
     for (int jj = 0; jj < jb; ++jj) {
       const int i = k0 + jj;
       const int nparts = cdiv(nmax - i, TR_NT);
-      k_colupd<R><<<dim3(nparts, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, w.d, sd, w.nrm, w.nrb);
+      PP_KT(KT_COLUPD, s, (k_colupd<R><<<dim3(nparts, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, w.d, sd, w.nrm, w.nrb)));
       if (i >= nmax - 1) {
         count_launch(1);
         continue;
       }
-      k_reflector<R><<<B, TR_NT, 0, s>>>(A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal);
+      PP_KT(KT_REFL, s, (k_reflector<R><<<B, TR_NT, 0, s>>>(A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal)));
       const int m = nmax - i - 1;
       dim3 gh(cdiv(m, HV_RB), cdiv(m, HV_CC), B);
-      k_hemv<R><<<gh, HV_RB, 0, s>>>(A, lda, sA, w.nvec, i, P, sP, lda);
-      if (jj > 0) k_dots<R><<<dim3(2 * jj, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb);
+      PP_KT(KT_HEMV, s, (k_hemv<R><<<gh, HV_RB, 0, s>>>(A, lda, sA, w.nvec, i, P, sP, lda)));
+      if (jj > 0) PP_KT(KT_DOTS, s, (k_dots<R><<<dim3(2 * jj, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb)));
       const int nr = cdiv(m, TR_NT);
-      k_wcorr<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, P, sP, lda, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb,
-                                               w.scal, (z64 *)w.wv, w.nrb);
-      k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nr, w.scal, (z64 *)w.wv, w.nrb);
+      PP_KT(KT_WCORR, s, (k_wcorr<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, P, sP, lda, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb,
+                                               w.scal, (z64 *)w.wv, w.nrb)));
+      PP_KT(KT_WFIN, s, (k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nr, w.scal, (z64 *)w.wv, w.nrb)));
       count_launch(jj > 0 ? 6 : 5);
     }
     const int k1 = k0 + jb;
     if (k1 < nmax) {
       const int m = nmax - k1;
       dim3 g(cdiv(m, HK_T), cdiv(m, HK_T), B);
-      k_her2k<R><<<g, 256, 0, s>>>(A, lda, sA, W, sW, w.nvec, k0, jb);
+      PP_KT(KT_HER2K, s, (k_her2k<R><<<g, 256, 0, s>>>(A, lda, sA, W, sW, w.nvec, k0, jb)));
       count_launch(1);
     }
   }
@@ -549,7 +549,7 @@ cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, in
     smem = 0;
   }
   dim3 g(cdiv(w.nmax, 128), w.B);
-  k_bisect<<<g, 128, smem, s>>>(w.d, w.e, sd, w.nvec, w.rng, w.tinfo, abstol, w.w, w.info, use_smem);
+  PP_KT(KT_BISECT, s, (k_bisect<<<g, 128, smem, s>>>(w.d, w.e, sd, w.nvec, w.rng, w.tinfo, abstol, w.w, w.info, use_smem)));
   count_launch(2);
   return cudaGetLastError();
 }
@@ -751,8 +751,8 @@ cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
   const int64_t sPv = (int64_t)w.nmax * T;
   for (int64_t cb = 0; cb < w.mcap; cb += T) {
     dim3 g(cdiv(T, 64), w.B);
-    k_invit<R><<<g, 64, 0, s>>>(w.d, w.e, sd, w.nvec, w.w, w.rng, w.tinfo, w.cls, scl, w.ncl, (int)cb, (C<R> *)w.E,
-                                w.lde, w.sE, w.scratch, w.piv, T, sS, sPv, w.info);
+    PP_KT(KT_INVIT, s, (k_invit<R><<<g, 64, 0, s>>>(w.d, w.e, sd, w.nvec, w.w, w.rng, w.tinfo, w.cls, scl, w.ncl, (int)cb, (C<R> *)w.E,
+                                w.lde, w.sE, w.scratch, w.piv, T, sS, sPv, w.info)));
     count_launch(1);
   }
   return cudaGetLastError();
@@ -965,15 +965,15 @@ cudaError_t back_transform(EigWork &w, cudaStream_t s) {
     const int jb = min(nb, nref - k0);
     const int ks = cdiv(nmax - k0 - 1, BT_RCH);
     // Tf from G = V^H V
-    k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, ldwp, sWp);
-    k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb, sWb);
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, ldwp, sWp)));
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb, sWb)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
     // Y = Tf V^H E ; E -= V Y
-    k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
-                                                             jb, Wp, ldwp, sWp);
-    k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb);
-    k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
-        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb);
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
+                                                             jb, Wp, ldwp, sWp)));
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb)));
+    PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
+        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb)));
     count_launch(6);
   }
   return cudaGetLastError();

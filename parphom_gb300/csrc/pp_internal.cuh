@@ -12,6 +12,23 @@ namespace pp {
 // Counts kernel launches made by this library (pp_kernel_launches()).
 void count_launch(int64_t k = 1);
 
+// Optional per-launch CUDA-event timing of selected kernel classes
+// (pp_ktimer_enable / pp_ktimer_report).
+enum KClass {
+  KT_ASSEMBLE = 0, KT_COLUPD, KT_REFL, KT_HEMV, KT_DOTS, KT_WCORR, KT_WFIN, KT_HER2K, KT_BISECT, KT_INVIT,
+  KT_VHX, KT_BTRED, KT_APPLYV, KT_VEL, KT_N
+};
+extern unsigned kt_mask;
+void kt_begin(int k, cudaStream_t s);
+void kt_end(int k, cudaStream_t s);
+#define PP_KT(k, s, launch)                         \
+  do {                                              \
+    const bool on__ = (pp::kt_mask >> (k)) & 1u;    \
+    if (on__) pp::kt_begin((k), (s));               \
+    launch;                                         \
+    if (on__) pp::kt_end((k), (s));                 \
+  } while (0)
+
 // Per-batch state of the eigensolver.  Every matrix b of a batch of `B`
 // Hermitian matrices has its own order nvec[b] <= nmax; all buffers use the
 // leading dimensions of the largest.  Complex buffers hold 16-byte elements:
