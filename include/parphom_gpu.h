@@ -44,6 +44,7 @@ typedef struct pp_ctx pp_ctx;
 #define PP_ERR_NODEVICE 1005  /* no CUDA device / kernel image not loadable    */
 #define PP_ERR_STATE 1006     /* context used after an unrecoverable error     */
 #define PP_ERR_UNSUPPORTED 1007
+#define PP_ERR_SIZE 1008      /* order beyond a fixed-capacity entry point    */
 
 /* Per-q info bits, as pzheevx INFO > 0 (diagonalize.F90:100-115). */
 #define PP_INFO_NOCONV 1      /* an eigenvalue failed to converge              */
@@ -151,6 +152,32 @@ PP_API int64_t pp_version(void);
 /* Number of kernels this library launched on the calling thread's contexts
  * since load (for launch accounting in benchmarks). */
 PP_API int64_t pp_kernel_launches(void);
+
+/* Largest matrix order pp_heevx_values_noalloc accepts. */
+#define PP_NOALLOC_MAX_N 1536
+
+/* Eigenvalues of one Hermitian matrix with no device allocation at all.
+ * No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory (inside a stream capture or a pipeline they do not
+ * own, drivers that hand over a fixed device pool).  The FP64 reduction and
+ * bisection use one fixed scratch array of about 1.5 MB compiled into the
+ * library, which every GPU that loads the library keeps until exit.
+ *   a_dev   n x n complex FP64 column-major device matrix, ld lda; only the
+ *           upper triangle is read (as pzheevx with uplo 'U'); overwritten.
+ *   n       1 <= n <= PP_NOALLOC_MAX_N, else PP_ERR_SIZE; lda <= 1536 too.
+ *   range   'A', 'I' (il..iu, 1-based) or 'V' (eigenvalues in (vl, vu],
+ *           bounds in the matrix's own units), abstol as in pzheevx.
+ *   w_dev   [n] eigenvalues ascending (first *m_dev valid); m_dev, info_dev
+ *           one int64 each (info: pzheevx-style bits); all device memory.
+ * Enqueued on `stream`.  The first call on a device resolves the array's
+ * address (cudaGetSymbolAddress) with that device current: make that first
+ * call before any stream capture.  All calls share the one array and leave
+ * their contents in it; calls that overlap on the GPU (different streams,
+ * threads or captured graphs running at once) race on it.  Do not enable
+ * pp_ktimer_enable around it (the timer creates CUDA events). */
+PP_API int pp_heevx_values_noalloc(double *a_dev, int64_t lda, int64_t n, char range, double vl, double vu,
+                                   int64_t il, int64_t iu, double abstol, double *w_dev, int64_t *m_dev,
+                                   int64_t *info_dev, void *stream);
 
 /* Instrumentation (no counterpart in the reference): record CUDA events
  * around every launch of the named kernel classes (comma separated, e.g.

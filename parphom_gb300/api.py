@@ -30,7 +30,10 @@ INFO_NOMEM = 4
 INFO_NOTCOMP = 8
 
 EXPORTED = ("pp_ctx_create", "pp_ctx_destroy", "pp_solve_batch", "pp_solve_batch_device", "pp_dynamical_matrix",
-            "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report")
+            "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report",
+            "pp_heevx_values_noalloc")
+PP_ERR_SIZE = 1008
+PP_NOALLOC_MAX_N = 1536
 
 _i64 = ctypes.c_int64
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -95,6 +98,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.pp_strerror.restype = ctypes.c_char_p
     L.pp_version.restype = _i64
     L.pp_kernel_launches.restype = _i64
+    L.pp_heevx_values_noalloc.argtypes = [ctypes.c_void_p, _i64, _i64, ctypes.c_char, ctypes.c_double,
+                                          ctypes.c_double, _i64, _i64, ctypes.c_double, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.pp_heevx_values_noalloc.restype = ctypes.c_int
     L.pp_ktimer_enable.argtypes = [ctypes.c_char_p]
     L.pp_ktimer_enable.restype = ctypes.c_int
     L.pp_ktimer_report.argtypes = [ctypes.c_char_p, _i64]
@@ -251,6 +258,22 @@ class PhononContext:
                                              ctypes.c_void_p(int(stream)))
         if rc != 0:
             raise PPError(rc, "pp_solve_batch_device")
+
+
+def heevx_values_noalloc(a_ptr: int, lda: int, n: int, w_ptr: int, m_ptr: int, info_ptr: int, range: str = "A",
+                         vl: float = 0.0, vu: float = 0.0, il: int = 1, iu: int = 1,
+                         abstol: float = float(np.float32(1e-15)), stream: int = 0) -> int:
+    """pp_heevx_values_noalloc on device pointers; returns the C return code.
+
+    For callers that cannot allocate device memory: the library allocates
+    nothing during the call (its scratch is a fixed array compiled into it,
+    n <= PP_NOALLOC_MAX_N).  The matrix at a_ptr (complex128, column-major,
+    upper triangle read) is overwritten."""
+    L = load()
+    return int(L.pp_heevx_values_noalloc(ctypes.c_void_p(a_ptr), int(lda), int(n), range.encode()[:1], float(vl),
+                                         float(vu), int(il), int(iu), float(abstol), ctypes.c_void_p(w_ptr),
+                                         ctypes.c_void_p(m_ptr), ctypes.c_void_p(info_ptr),
+                                         ctypes.c_void_p(int(stream))))
 
 
 def kernel_timer(names: str) -> None:

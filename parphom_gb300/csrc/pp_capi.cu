@@ -377,6 +377,7 @@ const char *pp_strerror(int code) {
     case PP_ERR_NODEVICE: return "no usable CUDA device for this library (sm_103a)";
     case PP_ERR_STATE: return "context is unusable after an earlier error";
     case PP_ERR_UNSUPPORTED: return "unsupported option";
+    case PP_ERR_SIZE: return "matrix order exceeds the fixed scratch capacity (PP_NOALLOC_MAX_N = 1536)";
     default:
       if (code < 0) return "illegal argument (index given by -code)";
       return "unknown error";
