@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi (profiler runs)")
-    p.add_argument("--roofline-kernels", default="hemv,her2k,vhx,applyV,invit,bisect,vel,assemble")
+    p.add_argument("--roofline-kernels", default="assemble,colupd,refl,hemv,dots,wcorr,wfin,her2k,bisect,invit,vhx,btred,applyV,vel")
     return p.parse_args()
 
 

@@ -143,6 +143,20 @@ PP_API int pp_solve_batch_device(pp_ctx *ctx, const double *q_dev, int64_t ldq, 
 PP_API int pp_dynamical_matrix(pp_ctx *ctx, const double *q, int64_t derivative, char vel_method, double *d,
                         int64_t ldd);
 
+/* Backward pass for the force constants (no counterpart in the reference;
+ * the differentiation layer of the Python package uses it).  For nq
+ * q-points in device memory (q_dev[3*t + k], reduced coordinates), their
+ * eigenvectors z_dev (FP64 complex, z[2*(r + ldz*j) + zstride*t], m
+ * columns) and weights wgt_dev[j + ldwgt*t] = dL/dlambda_j, adds to the
+ * symmetric n x n device matrix g_dev (column-major, ld n)
+ *   g(r,c) += sum_t Re(M_t(c,r) p_t(r,c)),  M_t = Z_t diag(wgt_t) Z_t^H,
+ * p_t being the phase/mass factor of D(q_t)(r,c) built from the upper
+ * triangle; i.e. dL/dPhi for a symmetric Phi.  precision PP_PREC_FP64 or
+ * PP_PREC_MIXED (double-float accumulation).  Enqueued on `stream`. */
+PP_API int pp_backward_phi(pp_ctx *ctx, const double *q_dev, int64_t nq, const double *z_dev, int64_t ldz,
+                           int64_t zstride, int64_t m, const double *wgt_dev, int64_t ldwgt, double *g_dev,
+                           int32_t precision, void *stream);
+
 /* Human-readable text for a return code. */
 PP_API const char *pp_strerror(int code);
 

@@ -31,7 +31,7 @@ INFO_NOTCOMP = 8
 
 EXPORTED = ("pp_ctx_create", "pp_ctx_destroy", "pp_solve_batch", "pp_solve_batch_device", "pp_dynamical_matrix",
             "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report",
-            "pp_heevx_values_noalloc")
+            "pp_heevx_values_noalloc", "pp_backward_phi")
 PP_ERR_SIZE = 1008
 PP_NOALLOC_MAX_N = 1536
 
@@ -102,6 +102,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                           ctypes.c_double, _i64, _i64, ctypes.c_double, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.pp_heevx_values_noalloc.restype = ctypes.c_int
+    L.pp_backward_phi.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _i64, ctypes.c_void_p, _i64, _i64, _i64,
+                                  ctypes.c_void_p, _i64, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
+    L.pp_backward_phi.restype = ctypes.c_int
     L.pp_ktimer_enable.argtypes = [ctypes.c_char_p]
     L.pp_ktimer_enable.restype = ctypes.c_int
     L.pp_ktimer_report.argtypes = [ctypes.c_char_p, _i64]

@@ -170,8 +170,8 @@ int ensure_ws(pp_ctx *c, int B, int mcap) {
   const int64_t n = c->g.n;
   const int nb = 32;
   const int64_t lda = (n + 7) / 8 * 8;
-  const int nchunk = (int)((n + 63) / 64);
-  const int nrb = (int)((n + 255) / 256) + 1;
+  const int nchunk = (int)((n + 31) / 32);
+  const int nrb = (int)((n + 31) / 32) + 1;  // partial sums per column kernel block
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
   const int ldwp = std::max(mcap, 64);
   const int ksplit = (int)((n + 511) / 512);
@@ -214,7 +214,7 @@ int ensure_ws(pp_ctx *c, int B, int mcap) {
   add((void **)&w.tinfo, 8 * (size_t)B * 8);
   add((void **)&w.cls, 4 * (size_t)B * (n + 1));
   add((void **)&w.ncl, 4 * (size_t)B);
-  add((void **)&w.scratch, 8 * (size_t)B * 4 * n * T);
+  add((void **)&w.scratch, 8 * (size_t)B * 5 * n * T);
   add((void **)&w.piv, (size_t)B * n * T);
   add((void **)&w.info, 8 * (size_t)B);
   add((void **)&w.Tf, 16 * (size_t)B * 1024);
@@ -248,7 +248,7 @@ int ensure_ws(pp_ctx *c, int B, int mcap) {
 
 size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd) {
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
-  size_t per = 16 * (size_t)n * n + 16 * (size_t)n * mcap + 8 * (size_t)4 * n * T + (size_t)n * T +
+  size_t per = 16 * (size_t)n * n + 16 * (size_t)n * mcap + 8 * (size_t)5 * n * T + (size_t)n * T +
                16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
                8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd;
   return per * B;
@@ -626,6 +626,29 @@ int pp_solve_batch_device(pp_ctx *c, const double *q_dev, int64_t ldq, int64_t n
     }
   }
   c->stream = saved;
+  return PP_OK;
+}
+
+int pp_backward_phi(pp_ctx *c, const double *q_dev, int64_t nq, const double *z_dev, int64_t ldz, int64_t zstride,
+                    int64_t m, const double *wgt_dev, int64_t ldwgt, double *g_dev, int32_t precision, void *stream) {
+  if (!c) return -1;
+  if (!q_dev && nq > 0) return -2;
+  if (nq < 0) return -3;
+  if (!z_dev && nq > 0) return -4;
+  const int64_t n = c->g.n;
+  if (ldz < n) return -5;
+  if (zstride < 2 * ldz * m) return -6;
+  if (m < 0 || m > n) return -7;
+  if (!wgt_dev && nq > 0) return -8;
+  if (ldwgt < m) return -9;
+  if (!g_dev) return -10;
+  if (precision != PP_PREC_FP64 && precision != PP_PREC_MIXED) return -11;
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  for (int64_t t = 0; t < nq; ++t) {
+    cudaError_t e = backward_phi(c->g, q_dev + 3 * t, (const z64 *)(z_dev + zstride * t), ldz, (int)m,
+                                 wgt_dev + ldwgt * t, g_dev, precision, s);
+    if (e != cudaSuccess) return cuda_err(e);
+  }
   return PP_OK;
 }
 

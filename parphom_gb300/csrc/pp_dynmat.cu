@@ -539,3 +539,103 @@ cudaError_t finalize_outputs(EigWork &w, int efmt, int raw_lambda, const double 
 }
 
 }  // namespace pp
+
+namespace pp {
+// ---------------------------------------------------------------------------
+// Backward pass for the force constants.
+//
+// For a loss L(w) of the frequencies, dL/dD(r,c) = M(c,r) with
+// M = sum_nu c_nu e_nu e_nu^H (Hellmann-Feynman; c_nu = dL/dlambda_nu).  D is
+// built from the upper triangle of Phi, D(r,c) = Phi(r,c) p(r,c) with the
+// phase/mass factor p of the assembly, so for the symmetric Phi the
+// reference uses, dL/dPhi(r,c) = dL/dPhi(c,r) = Re(M(c,r) p(r,c)) (half of the
+// pair derivative on each of the two entries).  This kernel adds that, for
+// one q, to G: one block per upper 64x64 tile (r <= c tiles), M from the
+// eigenvectors Z (FP64, column-major, ldz) and the weights wgt (m) in
+// arithmetic R, the phase recomputed from the tie-set table.
+constexpr int BW_T = 64, BW_K = 8;
+template <class R>
+__global__ void __launch_bounds__(256) k_bwd_phi(GeoDev g, const double *q, const z64 *Z, int64_t ldz, int m,
+                                                 const double *wgt, double *G) {
+  __shared__ cx<R> sR[BW_K][BW_T], sC[BW_K][BW_T];
+  if (blockIdx.x > blockIdx.y) return;  // upper tiles only (G is symmetric)
+  const int64_t n = g.n, N = g.N;
+  const int64_t r0 = (int64_t)blockIdx.x * BW_T, c0 = (int64_t)blockIdx.y * BW_T;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  cx<R> acc[4][4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int s = 0; s < 4; ++s) acc[p][s] = cz<R>();
+  for (int k0 = 0; k0 < m; k0 += BW_K) {
+    for (int e = threadIdx.x; e < BW_K * BW_T; e += 256) {
+      const int x = e % BW_T, y = e / BW_T;
+      const int k = k0 + y;
+      const int64_t rr = r0 + x, cc = c0 + x;
+      const double wk = k < m ? wgt[k] : 0.0;
+      z64 zr = (k < m && rr < n) ? Z[rr + ldz * k] : z64{0.0, 0.0};
+      z64 zc = (k < m && cc < n) ? Z[cc + ldz * k] : z64{0.0, 0.0};
+      sR[y][x] = cfrom64<R>(zr.re * wk, zr.im * wk);
+      sC[y][x] = cfrom64<R>(zc.re, -zc.im);
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int k = 0; k < BW_K; ++k) {
+      cx<R> a[4], bq[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        a[p] = sR[k][tx + 16 * p];
+        bq[p] = sC[k][ty + 16 * p];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int s = 0; s < 4; ++s) cmac(acc[p][s], a[p], bq[s]);
+    }
+    __syncthreads();
+  }
+  // acc[p][s] = M(r, c) for r = r0+tx+16p, c = c0+ty+16s ; need Re(M(c,r) p(r,c)) = Re(conj(M(r,c)) p(r,c))
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int64_t r = r0 + tx + 16 * p, c = c0 + ty + 16 * s;
+      if (r >= n || c >= n || r > c) continue;
+      const int64_t I = r / 3, J = c / 3;
+      const int64_t lo = I < J ? I : J, hi = I < J ? J : I;
+      const uint32_t mask = g.mask[I + N * J];
+      double pr = 0.0, pi = 0.0;
+      int mult = 0;
+      for (int l = 0; l < 9; ++l) {
+        if (!((mask >> l) & 1u)) continue;
+        const int i = l / 3 - 1;
+        const int j = l - 1 - 3 * (i + 1);
+        const double pp = prephase(q, g.crys, N, lo, hi, i, j);
+        double sn, cs;
+        sincos(-(__dmul_rn(2.0 * PI_REF, pp)), &sn, &cs);
+        pr += cs;
+        pi += sn;
+        ++mult;
+      }
+      const double inv = 1.0 / ((double)mult * sqrt(g.mass[lo] * g.mass[hi]));
+      pr *= inv;
+      pi *= inv;  // r <= c: upper orientation, no conjugation
+      const z64 Mrc = cto64(cfin(acc[p][s]));
+      const double val = Mrc.re * pr + Mrc.im * pi;  // Re(conj(M) p)
+      G[r + n * c] += val;
+      if (r != c) G[c + n * r] += val;
+    }
+}
+
+cudaError_t backward_phi(const Geometry &g, const double *d_q, const z64 *Z, int64_t ldz, int m, const double *wgt,
+                         double *G, int prec, cudaStream_t s) {
+  GeoDev gd{g.d_fc, g.d_crys, g.d_mass, g.d_mask, g.natom, g.n};
+  const int nt = cdiv(g.n, BW_T);
+  if (prec == 1)
+    k_bwd_phi<df><<<dim3(nt, nt), 256, 0, s>>>(gd, d_q, Z, ldz, m, wgt, G);
+  else
+    k_bwd_phi<double><<<dim3(nt, nt), 256, 0, s>>>(gd, d_q, Z, ldz, m, wgt, G);
+  count_launch(1);
+  return cudaGetLastError();
+}
+}  // namespace pp

@@ -9,7 +9,7 @@
 //     panel corrections) follows the zlatrd recurrence; after each panel the
 //     trailing matrix gets the rank-2nb update A -= V W^H + W V^H.  The full
 //     Hermitian square is kept so that every matrix-vector pass reads
-//     coalesced columns.  A = Q T Q^H with Q = H(0) H(1) ... H(n-2),
+//     coalesced columns (only its lower triangle is read after assembly).  A = Q T Q^H with Q = H(0) H(1) ... H(n-2),
 //     H(i) = I - tau_i v_i v_i^H.
 //  2. Eigenvalues of T by Sturm-count bisection, one thread per eigenvalue
 //     index, with the dstebz tolerance rule max(abstol, pivmin,
@@ -72,8 +72,7 @@ __device__ z64 block_sum_z(z64 v, double *sh) {
 // Stage 1: reduction to tridiagonal form
 // ===========================================================================
 constexpr int TR_NT = 256;   // threads of the column kernels
-constexpr int HV_RB = 128;   // rows per hemv block
-constexpr int HV_CC = 64;    // columns per hemv chunk
+constexpr int HV_CC = 32;    // hemv tile width = rows per partial-sum slot
 
 // A(i:n,i) -= V(i:n,0:jj) conj(W(i,0:jj))^T + W(i:n,0:jj) conj(V(i,0:jj))^T ;
 // d[i] = Re A(i,i) ; partial sums of |A(r,i)|^2 for r >= i+2.
@@ -178,37 +177,80 @@ __global__ void __launch_bounds__(TR_NT) k_reflector(C<R> *Ab, int64_t lda, int6
   if (threadIdx.x == 0) A[(i + 1) + lda * i] = cfrom64<R>(1.0, 0.0);
 }
 
-// P[chunk][r] = sum_{c in chunk} A(r,c) v(c), r,c in [i+1, n), v = A(i+1:n, i).
+// Lower-triangle Hermitian mat-vec y = A v on the trailing block [i+1, n):
+// one block per lower tile pair (R >= C) of HL_T x HL_T; the tile is read
+// once and gives both A_RC v_C (into slot C of the rows of R) and
+// A_RC^H v_R (into slot R of the rows of C).  Every row receives exactly one
+// partial per slot 0 .. ntiles-1, summed later by k_wcorr.  Small tiles and
+// blocks keep many blocks resident per SM, so tile loads of some blocks
+// overlap the (double-float) arithmetic of others.
+constexpr int HL_T = 32;
+constexpr int HL_LD = HL_T + 1;  // padded column stride of the shared tile
+constexpr int HL_NT = 128;
 template <class R>
-__global__ void __launch_bounds__(HV_RB) k_hemv(const C<R> *Ab, int64_t lda, int64_t sA, const int *nvec, int i,
-                                                C<R> *Pb, int64_t sP, int64_t ldp) {
-  __shared__ C<R> sv[HV_CC];
+__global__ void __launch_bounds__(HL_NT) k_hemv_lower(const C<R> *Ab, int64_t lda, int64_t sA, const int *nvec,
+                                                      int i, C<R> *Pb, int64_t sP, int64_t ldp) {
+  __shared__ C<R> tile[HL_T * HL_LD];  // tile[c * HL_LD + r]
+  __shared__ C<R> vR[HL_T], vC[HL_T];
+  __shared__ C<R> red[4][HL_T];
   const int b = blockIdx.z;
   const int n = nvec[b];
   const int r0 = i + 1;
-  const int c0 = r0 + blockIdx.y * HV_CC;
-  if (r0 >= n || c0 >= n) return;
+  const int p = blockIdx.x;
+  int Rt = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+  while ((Rt + 1) * (Rt + 2) / 2 <= p) ++Rt;
+  while (Rt * (Rt + 1) / 2 > p) --Rt;
+  const int Ct = p - Rt * (Rt + 1) / 2;
+  const int rt0 = r0 + Rt * HL_T, ct0 = r0 + Ct * HL_T;
+  if (rt0 >= n) return;
   const C<R> *A = Ab + b * sA;
-  for (int t = threadIdx.x; t < HV_CC; t += blockDim.x) {
-    int c = c0 + t;
-    sv[t] = (c < n) ? A[c + lda * i] : cz<R>();
+  const int tid = threadIdx.x;
+  if (tid < HL_T) {
+    const int rr = rt0 + tid;
+    vR[tid] = rr < n ? A[rr + lda * i] : cz<R>();
+  } else if (tid < 2 * HL_T) {
+    const int cc = ct0 + tid - HL_T;
+    vC[tid - HL_T] = cc < n ? A[cc + lda * i] : cz<R>();
+  }
+#pragma unroll
+  for (int e = tid; e < HL_T * HL_T; e += HL_NT) {
+    const int c = e / HL_T, r = e % HL_T;
+    const int rr = rt0 + r, cc = ct0 + c;
+    tile[c * HL_LD + r] = (rr < n && cc < n) ? A[rr + lda * cc] : cz<R>();
   }
   __syncthreads();
-  const int r = r0 + blockIdx.x * HV_RB + threadIdx.x;
-  if (r >= n) return;
-  const int cend = min(HV_CC, n - c0);
-  C<R> acc = cz<R>();
-  const C<R> *Ar = A + r + lda * c0;
-  int t = 0;
-  for (; t + 4 <= cend; t += 4) {
-    C<R> a0 = Ar[lda * (t + 0)], a1 = Ar[lda * (t + 1)], a2 = Ar[lda * (t + 2)], a3 = Ar[lda * (t + 3)];
-    cmac(acc, a0, sv[t + 0]);
-    cmac(acc, a1, sv[t + 1]);
-    cmac(acc, a2, sv[t + 2]);
-    cmac(acc, a3, sv[t + 3]);
+  const int lane = tid & (HL_T - 1), part = tid / HL_T;
+  constexpr int SPAN = HL_T / (HL_NT / HL_T);
+  const bool diag = (Rt == Ct);
+  {
+    C<R> acc = cz<R>();
+    const int r = lane;
+#pragma unroll
+    for (int c = part * SPAN; c < part * SPAN + SPAN; ++c) {
+      const C<R> a = (!diag || r >= c) ? tile[c * HL_LD + r] : cconj(tile[r * HL_LD + c]);
+      cmac(acc, a, vC[c]);
+    }
+    red[part][r] = cfin(acc);
   }
-  for (; t < cend; ++t) cmac(acc, Ar[lda * t], sv[t]);
-  Pb[b * sP + (int64_t)blockIdx.y * ldp + r] = cfin(acc);
+  __syncthreads();
+  if (part == 0 && rt0 + lane < n) {
+    C<R> s = cadd(cadd(red[0][lane], red[1][lane]), cadd(red[2][lane], red[3][lane]));
+    Pb[b * sP + (int64_t)Ct * ldp + rt0 + lane] = s;
+  }
+  if (diag) return;
+  __syncthreads();
+  {
+    C<R> acc = cz<R>();
+    const int c = lane;
+#pragma unroll
+    for (int r = part * SPAN; r < part * SPAN + SPAN; ++r) cmacc(acc, tile[c * HL_LD + r], vR[r]);
+    red[part][c] = cfin(acc);
+  }
+  __syncthreads();
+  if (part == 0 && ct0 + lane < n) {
+    C<R> s = cadd(cadd(red[0][lane], red[1][lane]), cadd(red[2][lane], red[3][lane]));
+    Pb[b * sP + (int64_t)Rt * ldp + ct0 + lane] = s;
+  }
 }
 
 // X[c] = V(:,c)^H v (c < jj), X[jj+c] = W(:,c)^H v, over rows [i+1, n).
@@ -232,6 +274,11 @@ __global__ void __launch_bounds__(TR_NT) k_dots(const C<R> *Ab, int64_t lda, int
 }
 
 // w = tau (y - W x1 - V x2) with y = sum of hemv partials; partial w^H v.
+// WC_TPR threads share one row: each sums a strided subset of the partial
+// slots, then a shuffle reduction; this keeps many independent loads in
+// flight per row (the slots are the latency-bound part).
+constexpr int WC_TPR = 8;
+constexpr int WC_ROWS = TR_NT / WC_TPR;  // rows per block
 template <class R>
 __global__ void __launch_bounds__(TR_NT) k_wcorr(const C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
                                                  const C<R> *Pb, int64_t sP, int64_t ldp, const int *nvec, int i,
@@ -249,12 +296,25 @@ __global__ void __launch_bounds__(TR_NT) k_wcorr(const C<R> *Ab, int64_t lda, in
     x2[c] = cfrom64<R>(X[b * ldx + jj + c]);  // W^H v
   }
   __syncthreads();
-  const int r = i + 1 + blockIdx.x * TR_NT + threadIdx.x;
+  const int sub = threadIdx.x % WC_TPR;
+  const int r = i + 1 + blockIdx.x * WC_ROWS + threadIdx.x / WC_TPR;
   z64 part{0.0, 0.0};
+  const int nch = cdiv_dev(n - i - 1, HV_CC);
+  C<R> y = cz<R>();
   if (r < n) {
-    const int nch = cdiv_dev(n - i - 1, HV_CC);
-    C<R> y = cz<R>();
-    for (int ch = 0; ch < nch; ++ch) y = cadd(y, Pb[b * sP + (int64_t)ch * ldp + r]);
+    for (int ch = sub; ch < nch; ch += WC_TPR) y = cadd(y, Pb[b * sP + (int64_t)ch * ldp + r]);
+  }
+  // reduce the WC_TPR partial sums of this row (lanes of one warp)
+#pragma unroll
+  for (int o = WC_TPR / 2; o > 0; o >>= 1) {
+    C<R> other;
+    float *dst = (float *)&other;
+    const float *src = (const float *)&y;
+#pragma unroll
+    for (int f = 0; f < (int)(sizeof(C<R>) / sizeof(float)); ++f) dst[f] = __shfl_xor_sync(0xffffffffu, src[f], o);
+    y = cadd(y, other);
+  }
+  if (r < n && sub == 0) {
     if (jj > 0) {
       C<R> acc = cz<R>();
       for (int c = 0; c < jj; ++c) {
@@ -311,6 +371,7 @@ __global__ void __launch_bounds__(256) k_her2k(C<R> *Ab, int64_t lda, int64_t sA
   const int b = blockIdx.z;
   const int n = nvec[b];
   const int k1 = k0 + jb;
+  if (blockIdx.x < blockIdx.y) return;  // only the lower triangle is kept
   const int r0 = k1 + blockIdx.x * HK_T, c0 = k1 + blockIdx.y * HK_T;
   if (r0 >= n || c0 >= n) return;
   C<R> *A = Ab + b * sA;
@@ -386,13 +447,15 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
       }
       PP_KT(KT_REFL, s, (k_reflector<R><<<B, TR_NT, 0, s>>>(A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal)));
       const int m = nmax - i - 1;
-      dim3 gh(cdiv(m, HV_RB), cdiv(m, HV_CC), B);
-      PP_KT(KT_HEMV, s, (k_hemv<R><<<gh, HV_RB, 0, s>>>(A, lda, sA, w.nvec, i, P, sP, lda)));
+      const int nt = cdiv(m, HL_T);
+      PP_KT(KT_HEMV, s, (k_hemv_lower<R><<<dim3(nt * (nt + 1) / 2, 1, B), HL_NT, 0, s>>>(A, lda, sA, w.nvec, i,
+                                                                                      P, sP, lda)));
       if (jj > 0) PP_KT(KT_DOTS, s, (k_dots<R><<<dim3(2 * jj, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb)));
       const int nr = cdiv(m, TR_NT);
-      PP_KT(KT_WCORR, s, (k_wcorr<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, P, sP, lda, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb,
+      const int nrw = cdiv(m, WC_ROWS);
+      PP_KT(KT_WCORR, s, (k_wcorr<R><<<dim3(nrw, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, P, sP, lda, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb,
                                                w.scal, (z64 *)w.wv, w.nrb)));
-      PP_KT(KT_WFIN, s, (k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nr, w.scal, (z64 *)w.wv, w.nrb)));
+      PP_KT(KT_WFIN, s, (k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nrw, w.scal, (z64 *)w.wv, w.nrb)));
       count_launch(jj > 0 ? 6 : 5);
     }
     const int k1 = k0 + jb;
@@ -586,7 +649,10 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
 // One thread per cluster of eigenvalues (clusters cbase .. cbase+T-1).
 // LU of T - lam I with partial pivoting: row k of U holds (u0,u1,u2) at
 // columns (k, k+1, k+2); l is the multiplier, piv marks a row interchange.
-// Scratch is interleaved by thread ([row][field][thread]) for coalescing.
+// The factors and the working vector x live in scratch interleaved by thread
+// ([row][field][thread]) so that a warp's accesses coalesce; the finished
+// vector is written to its column of E once.
+constexpr int IV_F = 5;  // u0, u1, u2, l, x
 template <class R>
 __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee, int64_t sd, const int *nvec,
                                               const double *ww, const int64_t *rng, const double *tinfo,
@@ -604,16 +670,17 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
   C<R> *E = Eb + b * sE;
   double *S = scratch + b * sS;
   uint8_t *PV = pivb + b * sPv;
-#define SU0(k) S[((int64_t)(k)*4 + 0) * T + t]
-#define SU1(k) S[((int64_t)(k)*4 + 1) * T + t]
-#define SU2(k) S[((int64_t)(k)*4 + 2) * T + t]
-#define SL(k) S[((int64_t)(k)*4 + 3) * T + t]
+#define SU0(k) S[((int64_t)(k)*IV_F + 0) * T + t]
+#define SU1(k) S[((int64_t)(k)*IV_F + 1) * T + t]
+#define SU2(k) S[((int64_t)(k)*IV_F + 2) * T + t]
+#define SL(k) S[((int64_t)(k)*IV_F + 3) * T + t]
+#define XS(k) S[((int64_t)(k)*IV_F + 4) * T + t]
 #define PIV(k) PV[(int64_t)(k)*T + t]
-#define XV(k) E[(k) + lde * j].re
   const double tnorm = tinfo[b * 8 + 2];
   const double eps = DBL_EPSILON * 0.5;
   const double pivtol = fmax(eps * tnorm, DBL_MIN);
   const int j0 = cls[b * scl + c], j1 = cls[b * scl + c + 1];
+  const int iters = (j1 - j0 > 1) ? 3 : 2;
   double lam_prev = 0.0;
   int bad = 0;
   for (int j = j0; j < j1; ++j) {
@@ -662,31 +729,30 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
     // ---- deterministic start vector in (-1, 1)
     const uint32_t seed = hash32((uint32_t)j * 2654435761u ^ (uint32_t)b * 40503u ^ 0x9e3779b9u);
     for (int k = 0; k < n; ++k) {
-      uint32_t h = hash32(seed + (uint32_t)k * 0x85ebca6bu);
-      double x = ((double)(h >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
-      E[k + lde * j] = cfrom64<R>(x, 0.0);
+      const uint32_t h = hash32(seed + (uint32_t)k * 0x85ebca6bu);
+      XS(k) = ((double)(h >> 8) * (1.0 / 16777216.0)) * 2.0 - 1.0;
     }
     bool ok = true;
-    for (int it = 0; it < 3 && ok; ++it) {
+    for (int it = 0; it < iters && ok; ++it) {
       // L solve with the recorded interchanges
-      double xk = RT<R>::to(XV(0));
+      double xk = XS(0);
       for (int k = 0; k < n - 1; ++k) {
-        const double xk1 = RT<R>::to(XV(k + 1));
+        const double xk1 = XS(k + 1);
         const double l = SL(k);
         if (PIV(k)) {
-          XV(k) = RT<R>::from(xk1);
+          XS(k) = xk1;
           xk = xk - l * xk1;
         } else {
-          XV(k) = RT<R>::from(xk);
+          XS(k) = xk;
           xk = xk1 - l * xk;
         }
       }
-      XV(n - 1) = RT<R>::from(xk);
+      XS(n - 1) = xk;
       // U solve
       double y1 = 0.0, y2 = 0.0, amax = 0.0;
       for (int k = n - 1; k >= 0; --k) {
-        const double y = (RT<R>::to(XV(k)) - SU1(k) * y1 - SU2(k) * y2) / SU0(k);
-        XV(k) = RT<R>::from(y);
+        const double y = (XS(k) - SU1(k) * y1 - SU2(k) * y2) / SU0(k);
+        XS(k) = y;
         amax = fmax(amax, fabs(y));
         y2 = y1;
         y1 = y;
@@ -696,48 +762,47 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
         break;
       }
       const double inv = 1.0 / amax;
-      for (int k = 0; k < n; ++k) XV(k) = RT<R>::from(RT<R>::to(XV(k)) * inv);
       // modified Gram-Schmidt against the earlier members of the cluster
       for (int pass = 0; pass < 2 && j > j0; ++pass) {
         for (int jp = j0; jp < j; ++jp) {
           double dot = 0.0;
-          for (int k = 0; k < n; ++k) dot += RT<R>::to(E[k + lde * jp].re) * RT<R>::to(XV(k));
-          for (int k = 0; k < n; ++k) XV(k) = RT<R>::from(RT<R>::to(XV(k)) - dot * RT<R>::to(E[k + lde * jp].re));
+          for (int k = 0; k < n; ++k) dot += RT<R>::to(E[k + lde * jp].re) * XS(k);
+          for (int k = 0; k < n; ++k) XS(k) = XS(k) - dot * RT<R>::to(E[k + lde * jp].re);
         }
       }
       double nrm2 = 0.0;
       for (int k = 0; k < n; ++k) {
-        const double v = RT<R>::to(XV(k));
+        const double v = XS(k) * inv;
         nrm2 += v * v;
       }
       if (!(nrm2 > 1e-280)) {
         ok = false;
         break;
       }
-      const double sc = 1.0 / sqrt(nrm2);
-      for (int k = 0; k < n; ++k) XV(k) = RT<R>::from(RT<R>::to(XV(k)) * sc);
+      const double sc = inv / sqrt(nrm2);
+      for (int k = 0; k < n; ++k) XS(k) = XS(k) * sc;
     }
     if (!ok) bad = 1;
     // sign convention of dstein: the largest component is positive
     double big = -1.0;
     int kb = 0;
     for (int k = 0; k < n; ++k) {
-      const double v = fabs(RT<R>::to(XV(k)));
+      const double v = fabs(XS(k));
       if (v > big) {
         big = v;
         kb = k;
       }
     }
-    const double sgn = RT<R>::to(XV(kb)) < 0.0 ? -1.0 : 1.0;
-    for (int k = 0; k < n; ++k) E[k + lde * j] = cfrom64<R>(RT<R>::to(XV(k)) * sgn, 0.0);
+    const double sgn = XS(kb) < 0.0 ? -1.0 : 1.0;
+    for (int k = 0; k < n; ++k) E[k + lde * j] = cfrom64<R>(XS(k) * sgn, 0.0);
   }
   if (bad) atomicOr((unsigned long long *)&info[b], (unsigned long long)PP_INFO_NOORTH);
 #undef SU0
 #undef SU1
 #undef SU2
 #undef SL
+#undef XS
 #undef PIV
-#undef XV
 }
 
 template <class R>
@@ -747,7 +812,7 @@ cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
   k_clusters<<<w.B, 32, 0, s>>>(w.w, sd, w.rng, w.tinfo, w.cls, scl, w.ncl);
   count_launch(1);
   const int64_t T = w.scratch_threads;
-  const int64_t sS = (int64_t)4 * w.nmax * T;
+  const int64_t sS = (int64_t)IV_F * w.nmax * T;
   const int64_t sPv = (int64_t)w.nmax * T;
   for (int64_t cb = 0; cb < w.mcap; cb += T) {
     dim3 g(cdiv(T, 64), w.B);

@@ -50,7 +50,7 @@ struct EigWork {
   void *X = nullptr;   // [B][2*nb]       V^H v and W^H v
   double *nrm = nullptr;  // [B][nrb]     partial column norms
   z64 *wv = nullptr;      // [B][nrb]     partial w^H v
-  int nrb = 0;            // row blocks for column kernels
+  int nrb = 0;            // partial-sum slots per matrix (>= row blocks of any column kernel)
   double *d = nullptr;    // [B][nmax] tridiagonal diagonal
   double *e = nullptr;    // [B][nmax] off-diagonal (real)
   z64 *tau = nullptr;     // [B][nmax] reflector scalars
@@ -62,7 +62,7 @@ struct EigWork {
   double *tinfo = nullptr;// [B][8]  gl, gu, tnorm, pivmin
   int *cls = nullptr;     // [B][nmax+1] cluster starts
   int *ncl = nullptr;     // [B]
-  double *scratch = nullptr; // inverse-iteration LU factors [B][4*nmax*T]
+  double *scratch = nullptr; // inverse-iteration LU factors and vector [B][5*nmax*T]
   uint8_t *piv = nullptr;    // inverse-iteration pivot flags [B][nmax*T]
   int64_t scratch_threads = 0;  // T: clusters handled per launch
   int64_t *info = nullptr;   // [B] info bits
@@ -110,6 +110,10 @@ cudaError_t assemble_deriv(const Geometry &g, const double *d_q, int derivative,
 cudaError_t velocities(const Geometry &g, const double *d_q, int B, const void *E, int64_t lde, int64_t sE,
                        int efmt, const int64_t *d_rng, int mmax, char method, double *d_vraw, double *d_part,
                        int nsplit, cudaStream_t s);
+
+// G(r,c) += Re(M(c,r) p(r,c)), M = Z diag(wgt) Z^H for one q (FP64 Z, m columns).
+cudaError_t backward_phi(const Geometry &g, const double *d_q, const z64 *Z, int64_t ldz, int m, const double *wgt,
+                         double *G, int prec, cudaStream_t s);
 
 // Eigen stages, templated on the real type (double / df) in pp_eigen.cu.
 template <class R>

@@ -21,8 +21,8 @@ namespace {
 constexpr int64_t NOALLOC_MAX_N = PP_NOALLOC_MAX_N;
 constexpr int64_t NB = 32;
 constexpr int64_t LDA_MAX = (NOALLOC_MAX_N + 7) / 8 * 8;
-constexpr int64_t NCHUNK_MAX = (NOALLOC_MAX_N + 63) / 64;
-constexpr int64_t NRB_MAX = (NOALLOC_MAX_N + 255) / 256 + 1;
+constexpr int64_t NCHUNK_MAX = (NOALLOC_MAX_N + 31) / 32;
+constexpr int64_t NRB_MAX = (NOALLOC_MAX_N + 31) / 32 + 1;
 
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // byte offsets of the scratch buffers inside the array
@@ -128,7 +128,7 @@ extern "C" PP_API int pp_heevx_values_noalloc(double *a_dev, int64_t lda, int64_
   w.sA = lda * n;
   w.W = base + OFF_W;
   w.P = base + OFF_P;
-  w.nchunk = (int)((n + 63) / 64);
+  w.nchunk = (int)((n + 31) / 32);
   w.X = base + OFF_X;
   w.nrm = (double *)(base + OFF_NRM);
   w.wv = (z64 *)(base + OFF_WV);

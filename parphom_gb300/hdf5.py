@@ -238,3 +238,205 @@ class File:
 
 def read_dataset(path: str, name: str) -> np.ndarray:
     return File(path)[name]
+
+
+# ---------------------------------------------------------------------------
+# Writer (superblock 0, symbol-table groups, version-1 object headers,
+# contiguous datasets) for the reference's output layout.
+UNDEF = 0xFFFFFFFFFFFFFFFF
+LEAF_K = 64         # a symbol-table node holds up to 2K entries
+INTERNAL_K = 64     # a group B-tree node holds up to 2K children (one level: <= 16384 members)
+
+
+def _pad8(b: bytes) -> bytes:
+    return b + b"\x00" * ((-len(b)) % 8)
+
+
+def _msg(mtype: int, body: bytes, flags: int = 0) -> bytes:
+    body = _pad8(body)
+    return struct.pack("<HHB3x", mtype, len(body), flags) + body
+
+
+def _dt_f64() -> bytes:
+    # class 1 (floating point), version 1; little endian, implied MSB, sign at bit 63
+    return struct.pack("<B3BI", 0x11, 0x20, 0x3F, 0x00, 8) + struct.pack("<HHBBBBI", 0, 64, 52, 11, 0, 52, 1023)
+
+
+def _dt_i64() -> bytes:
+    # class 0 (fixed point), version 1, little endian, signed
+    return struct.pack("<B3BI", 0x10, 0x08, 0x00, 0x00, 8) + struct.pack("<HH", 0, 64)
+
+
+def _dt_compound(members) -> bytes:
+    """members: [(name, offset)] of float64 fields, version-1 compound."""
+    size = 8 * len(members)
+    out = struct.pack("<BHBI", 0x16, len(members), 0, size)
+    for name, off in members:
+        out += _pad8(name.encode() + b"\x00")
+        out += struct.pack("<IB3xI4x4I", off, 0, 0, 0, 0, 0, 0)
+        out += _dt_f64()
+    return out
+
+
+class _Writer:
+    """Appends objects to a file; the superblock is written last."""
+
+    def __init__(self, f):
+        self.f = f
+        self.pos = 96
+        f.write(b"\x00" * 96)
+
+    def alloc(self, data) -> int:
+        pad = (-self.pos) % 8
+        if pad:
+            self.f.write(b"\x00" * pad)
+            self.pos += pad
+        addr = self.pos
+        self.f.write(data)
+        self.pos += len(data)
+        return addr
+
+    def object_header(self, messages) -> int:
+        body = b"".join(messages)
+        hdr = struct.pack("<BBHII4x", 1, 0, len(messages), 1, len(body))
+        return self.alloc(hdr + body)
+
+    def dataset(self, arr: np.ndarray, dtype_msg: bytes) -> int:
+        raw = memoryview(np.ascontiguousarray(arr)).cast("B")
+        data_addr = self.alloc(raw) if len(raw) else UNDEF
+        shape = arr.shape
+        space = struct.pack("<BBBx4x", 1, len(shape), 0) + b"".join(struct.pack("<Q", d) for d in shape)
+        layout = struct.pack("<BBQQ", 3, 1, data_addr, len(raw))
+        return self.object_header([_msg(0x0001, space), _msg(0x0003, dtype_msg, flags=1), _msg(0x0008, layout)])
+
+    def group(self, entries) -> int:
+        """entries: sorted list of (name, header_addr, is_group, (btree, heap) or None)."""
+        btree, heap = self.symbol_table(entries)
+        return self.object_header([_msg(0x0011, struct.pack("<QQ", btree, heap))]), btree, heap
+
+    def symbol_table(self, entries):
+        entries = sorted(entries, key=lambda e: e[0].encode())
+        heapdata = bytearray(b"\x00" * 8)     # offset 0: the empty name
+        offs = []
+        for e in entries:
+            offs.append(len(heapdata))
+            heapdata += _pad8(e[0].encode() + b"\x00")
+        data_addr = self.alloc(bytes(heapdata))
+        heap_addr = self.alloc(b"HEAP" + struct.pack("<B3xQQQ", 0, len(heapdata), UNDEF, data_addr))
+        # symbol-table nodes of at most 2*LEAF_K entries each
+        cap = 2 * LEAF_K
+        chunks = [list(range(i, min(i + cap, len(entries)))) for i in range(0, max(len(entries), 1), cap)]
+        if not entries:
+            chunks = [[]]
+        snods = []
+        for ch in chunks:
+            node = bytearray(b"SNOD" + struct.pack("<BBH", 1, 0, len(ch)))
+            for k in ch:
+                name, hdr, is_grp, scratch = entries[k]
+                if is_grp:
+                    node += struct.pack("<QQI4xQQ", offs[k], hdr, 1, scratch[0], scratch[1])
+                else:
+                    node += struct.pack("<QQI4x16x", offs[k], hdr, 0)
+            node += b"\x00" * (40 * (cap - len(ch)))
+            snods.append(self.alloc(bytes(node)))
+        if len(snods) > 2 * INTERNAL_K:
+            raise HDF5Error("too many group members for a one-level group B-tree")
+        tree = bytearray(b"TREE" + struct.pack("<BBHQQ", 0, 0, len(snods), UNDEF, UNDEF))
+        tree += struct.pack("<Q", 0)
+        for i, (s, ch) in enumerate(zip(snods, chunks)):
+            last = offs[ch[-1]] if ch else 0
+            tree += struct.pack("<QQ", s, last)
+        tree += b"\x00" * (16 * (2 * INTERNAL_K - len(snods)))
+        btree_addr = self.alloc(bytes(tree))
+        return btree_addr, heap_addr
+
+    def close(self, root_entries) -> None:
+        root_hdr, btree, heap = self.group(root_entries)
+        sb = bytearray(SIG + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", LEAF_K, INTERNAL_K, 0))
+        sb += struct.pack("<QQQQ", 0, UNDEF, self.pos, UNDEF)
+        sb += struct.pack("<QQI4xQQ", 0, root_hdr, 1, btree, heap)
+        assert len(sb) == 96
+        self.f.seek(0)
+        self.f.write(bytes(sb))
+
+
+class Writer:
+    """Streaming writer: `add_group(name, datasets)` writes one group and its
+    datasets immediately; `close()` writes the root group and superblock.
+    Used for the per-q output groups, which can be large (eigenvectors)."""
+
+    def __init__(self, path: str):
+        self._f = open(path, "wb")
+        self._w = _Writer(self._f)
+        self._root = []
+
+    def add_group(self, name: str, datasets: dict) -> None:
+        ents = []
+        for k, v in datasets.items():
+            ents.append((k, _write_dataset(self._w, v), False, None))
+        hdr, bt, hp = self._w.group(ents)
+        self._root.append((name, hdr, True, (bt, hp)))
+
+    def add_dataset(self, name: str, value) -> None:
+        self._root.append((name, _write_dataset(self._w, value), False, None))
+
+    def close(self) -> None:
+        if self._f is None:
+            return
+        try:
+            self._w.close(self._root)
+        finally:
+            self._f.close()
+            self._f = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def _write_dataset(w: _Writer, v) -> int:
+    a = np.asarray(v)
+    if np.iscomplexobj(a):
+        rec = np.empty(a.shape, dtype=[("r", "<f8"), ("i", "<f8")])
+        rec["r"], rec["i"] = a.real, a.imag
+        return w.dataset(rec, _dt_compound([("r", 0), ("i", 8)]))
+    if a.dtype.kind in "iu":
+        return w.dataset(a.astype("<i8"), _dt_i64())
+    return w.dataset(a.astype("<f8"), _dt_f64())
+
+
+def write_file(path: str, tree: dict) -> None:
+    """Write nested dict {group: {name: ndarray | dict}} as HDF5.  float64
+    arrays become IEEE F64LE datasets, int64 arrays I64LE, complex128 arrays
+    the reference's compound {r: f64, i: f64} type."""
+    f = open(path, "wb")
+    w = _Writer(f)
+
+    def build(d):
+        ents = []
+        for name, v in d.items():
+            if isinstance(v, dict):
+                hdr, bt, hp = build_group(v)
+                ents.append((name, hdr, True, (bt, hp)))
+            else:
+                a = np.asarray(v)
+                if np.iscomplexobj(a):
+                    rec = np.empty(a.shape, dtype=[("r", "<f8"), ("i", "<f8")])
+                    rec["r"], rec["i"] = a.real, a.imag
+                    hdr = w.dataset(rec, _dt_compound([("r", 0), ("i", 8)]))
+                elif a.dtype.kind in "iu":
+                    hdr = w.dataset(a.astype("<i8"), _dt_i64())
+                else:
+                    hdr = w.dataset(a.astype("<f8"), _dt_f64())
+                ents.append((name, hdr, False, None))
+        return ents
+
+    def build_group(d):
+        return w.group(build(d))
+
+    try:
+        w.close(build(tree))
+    finally:
+        f.close()
