@@ -19,7 +19,7 @@ void count_launch(int64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed
 
 unsigned kt_mask = 0;
 static const char *kt_names[KT_N] = {"assemble", "colupd", "refl", "hemv", "dots", "wcorr", "wfin", "her2k",
-                                     "bisect", "invit", "vhx", "btred", "applyV", "vel"};
+                                     "bisect", "invit", "vhx", "btred", "applyV", "vel", "xhz"};
 struct KtPending {
   int k;
   cudaEvent_t a, b;
@@ -173,7 +173,8 @@ int ensure_ws(pp_ctx *c, int B, int mcap) {
   const int nchunk = (int)((n + 31) / 32);
   const int nrb = (int)((n + 31) / 32) + 1;  // partial sums per column kernel block
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
-  const int ldwp = std::max(mcap, 64);
+  const int nbr = (int)c->g.nbrows;
+  const int ldwp = std::max(std::max(mcap, nbr), 64);
   const int ksplit = (int)((n + 511) / 512);
   const int64_t nbnd = c->g.nbnd;
   std::vector<std::pair<void **, size_t>> parts;
@@ -221,6 +222,9 @@ int ensure_ws(pp_ctx *c, int B, int mcap) {
   add((void **)&w.G, 16 * (size_t)B * 1024);
   add(&w.Wb, 16 * (size_t)B * 32 * ldwp);
   add(&w.Wp, 16 * (size_t)B * ksplit * 32 * ldwp);
+  w.nbr = nbr;
+  add(&w.Xr, 16 * (size_t)B * lda * std::max(nbr, 1));
+  add(&w.Eb, 16 * (size_t)B * std::max(nbr, 1) * mcap);
   add((void **)&c->vpart, 8 * (size_t)B * c->nsplit * 3 * mcap + 16 * (size_t)B * nbnd * 3);
   add((void **)&c->vraw, 8 * (size_t)B * 3 * mcap);
   add((void **)&c->d_q, 8 * (size_t)B * 3);
@@ -246,11 +250,11 @@ int ensure_ws(pp_ctx *c, int B, int mcap) {
   return PP_OK;
 }
 
-size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd) {
+size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd, int64_t nbr) {
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
   size_t per = 16 * (size_t)n * n + 16 * (size_t)n * mcap + 8 * (size_t)5 * n * T + (size_t)n * T +
                16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
-               8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd;
+               8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd + 16 * (size_t)nbr * (n + mcap);
   return per * B;
 }
 
@@ -269,7 +273,7 @@ int check_opts(const pp_ctx *c, const pp_eig_opts *o) {
 
 // Run the pipeline for B q-points already in c->d_q; results left in the
 // EigWork buffers, velocities in c->vraw.
-int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap) {
+int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   EigWork &w = c->w;
   w.B = B;
   cudaStream_t s = c->stream;
@@ -283,16 +287,29 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap) {
   TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s));
   (void)mcap;
   if (vecs) {
+    // Velocities without eigenvector output need only the eigenvector rows
+    // of atoms in boundary blocks: back-transform those rows only.
+    const bool rows_only = o->vel && !want_z && c->g.nbrows < c->g.n;
     if (prec == PP_PREC_MIXED) {
       TRY_CUDA(tridiag_eigenvectors<df>(w, s));
-      TRY_CUDA(back_transform<df>(w, s));
+      if (rows_only)
+        TRY_CUDA(back_transform_rows<df>(w, c->g.d_brows, (int)c->g.nbrows, s));
+      else
+        TRY_CUDA(back_transform<df>(w, s));
     } else {
       TRY_CUDA(tridiag_eigenvectors<double>(w, s));
-      TRY_CUDA(back_transform<double>(w, s));
+      if (rows_only)
+        TRY_CUDA(back_transform_rows<double>(w, c->g.d_brows, (int)c->g.nbrows, s));
+      else
+        TRY_CUDA(back_transform<double>(w, s));
     }
     if (o->vel) {
-      TRY_CUDA(velocities(c->g, c->d_q, B, w.E, w.lde, w.sE, prec == PP_PREC_MIXED ? 1 : 0, w.rng, w.mcap,
-                          o->vel_method, c->vraw, c->vpart, c->nsplit, s));
+      if (rows_only)
+        TRY_CUDA(velocities(c->g, c->d_q, B, w.Eb, w.nbr, (int64_t)w.nbr * w.mcap, prec == PP_PREC_MIXED ? 1 : 0,
+                            w.rng, w.mcap, o->vel_method, c->vraw, c->vpart, c->nsplit, c->g.d_rowmap, s));
+      else
+        TRY_CUDA(velocities(c->g, c->d_q, B, w.E, w.lde, w.sE, prec == PP_PREC_MIXED ? 1 : 0, w.rng, w.mcap,
+                            o->vel_method, c->vraw, c->vpart, c->nsplit, nullptr, s));
     }
   }
   return PP_OK;
@@ -310,7 +327,7 @@ int pick_batch(pp_ctx *c, int64_t nq, int mcap) {
   if (c->ws) fr += c->ws_bytes;
   const size_t budget = (size_t)(0.6 * (double)fr);
   int B = (int)std::min<int64_t>(nq, 64);
-  while (B > 1 && ws_bytes_estimate(c->g.n, B, mcap, c->g.nbnd) > budget) B = B / 2;
+  while (B > 1 && ws_bytes_estimate(c->g.n, B, mcap, c->g.nbnd, c->g.nbrows) > budget) B = B / 2;
   const char *env = getenv("PARPHOM_GPU_BATCH");
   if (env) {
     int v = atoi(env);
@@ -476,6 +493,26 @@ int pp_ctx_create(const pp_system *sys, const double *fc, int64_t ldfc, int64_t 
       }
     }
   g.nbnd = (int64_t)bnd.size();
+  // rows of the atoms that appear in boundary blocks (all the velocity
+  // kernel reads of the eigenvectors)
+  std::vector<int> rows, rowmap(n, -1);
+  {
+    std::vector<char> used(N, 0);
+    for (auto &p : bnd) used[p.x] = used[p.y] = 1;
+    for (int64_t I = 0; I < N; ++I)
+      if (used[I])
+        for (int a = 0; a < 3; ++a) {
+          rowmap[3 * I + a] = (int)rows.size();
+          rows.push_back((int)(3 * I + a));
+        }
+  }
+  g.nbrows = (int64_t)rows.size();
+  if (cudaMalloc(&g.d_rowmap, sizeof(int) * n) != cudaSuccess) return fail(PP_ERR_NOMEM);
+  cudaMemcpy(g.d_rowmap, rowmap.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+  if (g.nbrows) {
+    if (cudaMalloc(&g.d_brows, sizeof(int) * g.nbrows) != cudaSuccess) return fail(PP_ERR_NOMEM);
+    cudaMemcpy(g.d_brows, rows.data(), sizeof(int) * g.nbrows, cudaMemcpyHostToDevice);
+  }
   if (g.nbnd) {
     if (cudaMalloc(&g.d_bnd, sizeof(int2) * g.nbnd) != cudaSuccess) return fail(PP_ERR_NOMEM);
     if (cudaMalloc(&g.d_bndmask, sizeof(uint16_t) * g.nbnd) != cudaSuccess) return fail(PP_ERR_NOMEM);
@@ -499,6 +536,8 @@ int pp_ctx_destroy(pp_ctx *c) {
   cudaFree(c->g.d_mask);
   cudaFree(c->g.d_bnd);
   cudaFree(c->g.d_bndmask);
+  cudaFree(c->g.d_brows);
+  cudaFree(c->g.d_rowmap);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PP_OK;
@@ -535,7 +574,7 @@ int pp_solve_batch(pp_ctx *c, const double *q, int64_t ldq, int64_t nq, const pp
     for (int b = 0; b < Bb; ++b)
       for (int k = 0; k < 3; ++k) qh[3 * b + k] = q[(t0 + b) + ldq * k];
     TRY_CUDA(cudaMemcpyAsync(c->d_q, qh.data(), sizeof(double) * 3 * Bb, cudaMemcpyHostToDevice, s));
-    r = run_batch(c, Bb, o, mcap);
+    r = run_batch(c, Bb, o, mcap, want_z);
     if (r) {
       c->broken = 1;
       return r;
@@ -609,7 +648,7 @@ int pp_solve_batch_device(pp_ctx *c, const double *q_dev, int64_t ldq, int64_t n
     for (int k = 0; k < 3; ++k)
       TRY_CUDA(cudaMemcpy2DAsync(c->d_q + k, 3 * sizeof(double), q_dev + t0 + ldq * k, sizeof(double),
                                  sizeof(double), Bb, cudaMemcpyDeviceToDevice, s));
-    r = run_batch(c, Bb, o, mcap);
+    r = run_batch(c, Bb, o, mcap, want_z);
     if (r) {
       c->stream = saved;
       c->broken = 1;

@@ -386,7 +386,8 @@ __device__ __forceinline__ z64 ld_e(const void *E, int64_t off) {
 template <int EFMT>
 __global__ void __launch_bounds__(128) k_vel(const int2 *bnd, int64_t nbnd, const double *fc, int64_t n,
                                             const z64 *gtab, const void *E, int64_t lde, int64_t sE,
-                                            const int64_t *rng, int nsplit, int64_t mstride, double *part) {
+                                            const int64_t *rng, int nsplit, int64_t mstride, double *part,
+                                            const int *rowmap) {
   const int b = blockIdx.z;
   const int split = blockIdx.y;
   const int64_t m = rng[b * 8 + 2];
@@ -401,11 +402,17 @@ __global__ void __launch_bounds__(128) k_vel(const int2 *bnd, int64_t nbnd, cons
     for (int64_t t = t0; t < t1; ++t) {
       const int2 p = bnd[t];
       if (p.x != lastI) {
-        for (int a = 0; a < 3; ++a) eI[a] = ld_e<EFMT>(E, col + 3 * (int64_t)p.x + a);
+        for (int a = 0; a < 3; ++a) {
+          const int64_t r = 3 * (int64_t)p.x + a;
+          eI[a] = ld_e<EFMT>(E, col + (rowmap ? rowmap[r] : r));
+        }
         lastI = p.x;
       }
       z64 eJ[3];
-      for (int a = 0; a < 3; ++a) eJ[a] = ld_e<EFMT>(E, col + 3 * (int64_t)p.y + a);
+      for (int a = 0; a < 3; ++a) {
+        const int64_t r = 3 * (int64_t)p.y + a;
+        eJ[a] = ld_e<EFMT>(E, col + (rowmap ? rowmap[r] : r));
+      }
       z64 h{0.0, 0.0};
       for (int a = 0; a < 3; ++a) {
         double fr = 0.0, fi = 0.0;
@@ -444,7 +451,7 @@ __global__ void k_vel_reduce(const double *part, int nsplit, int64_t mstride, co
 
 cudaError_t velocities(const Geometry &g, const double *d_q, int B, const void *E, int64_t lde, int64_t sE, int efmt,
                        const int64_t *d_rng, int mmax, char method, double *d_vraw, double *d_part, int nsplit,
-                       cudaStream_t s) {
+                       const int *rowmap, cudaStream_t s) {
   // d_part must hold B*nsplit*3*mmax doubles plus the gtab (B*nbnd*3 z64) after it
   const int64_t mstride = mmax;
   if (g.nbnd == 0) {
@@ -462,9 +469,9 @@ cudaError_t velocities(const Geometry &g, const double *d_q, int B, const void *
                                                          va, d_q, method, gtab);
   dim3 grid(cdiv(mmax, 128), nsplit, B);
   if (efmt == 0)
-    PP_KT(KT_VEL, s, (k_vel<0><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part)));
+    PP_KT(KT_VEL, s, (k_vel<0><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part, rowmap)));
   else
-    PP_KT(KT_VEL, s, (k_vel<1><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part)));
+    PP_KT(KT_VEL, s, (k_vel<1><<<grid, 128, 0, s>>>(g.d_bnd, g.nbnd, g.d_fc, g.n, gtab, E, lde, sE, d_rng, nsplit, mstride, d_part, rowmap)));
   k_vel_reduce<<<dim3(cdiv(mmax, 128), B), 128, 0, s>>>(d_part, nsplit, mstride, d_rng, d_vraw);
   count_launch(3);
   return cudaGetLastError();

@@ -545,6 +545,23 @@ __global__ void k_tdprep(const double *dd, const double *ee, int64_t sd, const i
   info[b] = 0;
 }
 
+__device__ __forceinline__ int sturm_count32(const float *d, const float *e2, int n, float x, float pivmin) {
+  float q = d[0] - x;
+  if (fabsf(q) <= pivmin) q = -pivmin;
+  int c = q < 0.0f;
+  for (int k = 1; k < n; ++k) {
+    q = d[k] - __fdividef(e2[k - 1], q) - x;
+    if (fabsf(q) <= pivmin) q = -pivmin;
+    c += q < 0.0f;
+  }
+  return c;
+}
+
+// One thread per wanted eigenvalue.  With the tridiagonal in shared memory
+// the interval is first narrowed with FP32 Sturm counts (cheap on the FP32
+// pipes), then widened by a margin far above the FP32 backward error of the
+// count (64 eps32 (||T|| + |x|)), checked with two FP64 counts (falling back to
+// the Gerschgorin interval if the check fails) and finished in FP64.
 __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *ee, int64_t sd, const int *nvec,
                                                 const int64_t *rng, const double *tinfo, double abstol, double *wout,
                                                 int64_t *info, int use_smem) {
@@ -555,10 +572,15 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
   const double *e = ee + b * sd;
   double *sd_ = sm;
   double *se2 = sm + n;
+  float *fd = (float *)(sm + 2 * n);
+  float *fe2 = fd + n;
   if (use_smem) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const double e2 = (k < n - 1) ? e[k] * e[k] : 0.0;
       sd_[k] = d[k];
-      se2[k] = (k < n - 1) ? e[k] * e[k] : 0.0;
+      se2[k] = e2;
+      fd[k] = (float)d[k];
+      fe2[k] = (float)e2;
     }
     __syncthreads();
   }
@@ -567,9 +589,40 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
   const int64_t idx = lo_idx + j;
+  const double gl = tinfo[b * 8 + 0], gu = tinfo[b * 8 + 1], tnorm = tinfo[b * 8 + 2];
   const double pivmin = tinfo[b * 8 + 3];
-  double lo = tinfo[b * 8 + 0], hi = tinfo[b * 8 + 1];
+  double lo = gl, hi = gu;
   const double ulp = DBL_EPSILON;
+  auto count64 = [&](double x) -> int {
+    if (use_smem) return sturm_count(sd_, se2, n, x, pivmin);
+    double q = d[0] - x;
+    if (fabs(q) <= pivmin) q = -pivmin;
+    int c = q < 0.0;
+    for (int k = 1; k < n; ++k) {
+      q = d[k] - (e[k - 1] * e[k - 1]) / q - x;
+      if (fabs(q) <= pivmin) q = -pivmin;
+      c += q < 0.0;
+    }
+    return c;
+  };
+  if (use_smem && tnorm > 0.0 && tnorm < 1e30) {
+    float lo32 = (float)lo, hi32 = (float)hi;
+    const float piv32 = fmaxf(1e-30f, (float)pivmin);
+    const float stop = 16.0f * FLT_EPSILON * (float)tnorm;
+    for (int it = 0; it < 48 && hi32 - lo32 > stop; ++it) {
+      const float mid = 0.5f * (lo32 + hi32);
+      if (sturm_count32(fd, fe2, n, mid, piv32) >= idx)
+        hi32 = mid;
+      else
+        lo32 = mid;
+    }
+    const double marg = 64.0 * FLT_EPSILON * (tnorm + fmax(fabs((double)lo32), fabs((double)hi32)));
+    const double l2 = fmax(gl, (double)lo32 - marg), h2 = fmin(gu, (double)hi32 + marg);
+    if (count64(l2) < idx && count64(h2) >= idx) {
+      lo = l2;
+      hi = h2;
+    }
+  }
   bool conv = false;
   for (int it = 0; it < 256; ++it) {
     double tol = fmax(fmax(abstol, pivmin), 2.0 * ulp * fmax(fabs(lo), fabs(hi)));
@@ -578,20 +631,7 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
       break;
     }
     double mid = 0.5 * (lo + hi);
-    int c;
-    if (use_smem)
-      c = sturm_count(sd_, se2, n, mid, pivmin);
-    else {
-      double q = d[0] - mid;
-      if (fabs(q) <= pivmin) q = -pivmin;
-      c = q < 0.0;
-      for (int k = 1; k < n; ++k) {
-        q = d[k] - (e[k - 1] * e[k - 1]) / q - mid;
-        if (fabs(q) <= pivmin) q = -pivmin;
-        c += q < 0.0;
-      }
-    }
-    if (c >= idx)
+    if (count64(mid) >= idx)
       hi = mid;
     else
       lo = mid;
@@ -604,7 +644,7 @@ cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, in
                                 cudaStream_t s) {
   const int64_t sd = w.nmax;
   k_tdprep<<<w.B, 32, 0, s>>>(w.d, w.e, sd, w.nvec, range, vl, vu, il, iu, w.rng, w.tinfo, w.info);
-  size_t smem = 2 * (size_t)w.nmax * sizeof(double);
+  size_t smem = 2 * (size_t)w.nmax * (sizeof(double) + sizeof(float));
   int use_smem = smem <= 200 * 1024;
   if (use_smem) {
     PP_CUDA_TRY(cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -836,12 +876,12 @@ constexpr int BT_RCH = 512;  // rows per split-K chunk
 template <class R>
 __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Xb, int64_t ldx,
                                              int64_t sX, int x_is_v, const int *nvec, const int64_t *rng, int k0,
-                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp) {
+                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp, int ncol_fixed) {
   __shared__ C<R> sV[BT_RK][32];
   __shared__ C<R> sXt[BT_RK][BT_J];
   const int b = blockIdx.z;
   const int n = nvec[b];
-  const int ncol = x_is_v ? jb : (int)rng[b * 8 + 2];
+  const int ncol = x_is_v ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
   const int j0 = blockIdx.x * BT_J;
   const int ks = blockIdx.y;
   const int rbeg = k0 + 1 + ks * BT_RCH;
@@ -891,14 +931,14 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
 template <class R>
 __global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int64_t sWp, const int *nvec,
                                               const int64_t *rng, int k0, int jb, int mode, z64 *G, const z64 *Tf,
-                                              C<R> *Wb, int64_t sWb) {
+                                              C<R> *Wb, int64_t sWb, int ncol_fixed) {
   __shared__ C<R> col[32][64];
   __shared__ z64 sT[32][32];
   const int b = blockIdx.y;
   const int n = nvec[b];
-  const int ncol = mode == 0 ? jb : (int)rng[b * 8 + 2];
+  const int ncol = mode == 0 ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
   const int nks = (n - k0 - 1 + BT_RCH - 1) / BT_RCH;
-  if (mode == 1) {
+  if (mode != 0) {
     for (int e = threadIdx.x; e < 32 * 32; e += 64) sT[e / 32][e % 32] = Tf[b * 1024 + e];
   }
   __syncthreads();
@@ -915,7 +955,11 @@ __global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int6
   }
   for (int a = 0; a < jb; ++a) {
     C<R> acc = cz<R>();
-    for (int a2 = a; a2 < jb; ++a2) cmac(acc, cfrom64<R>(sT[a][a2]), col[a2][threadIdx.x]);
+    if (mode == 1) {
+      for (int a2 = a; a2 < jb; ++a2) cmac(acc, cfrom64<R>(sT[a][a2]), col[a2][threadIdx.x]);
+    } else {  // mode 2: Tf^H (lower triangular)
+      for (int a2 = 0; a2 <= a; ++a2) cmac(acc, cfrom64<R>(zconj(sT[a2][a])), col[a2][threadIdx.x]);
+    }
     Wb[b * sWb + (int64_t)a * ldwp + j] = cfin(acc);
   }
 }
@@ -959,12 +1003,12 @@ constexpr int AV_T = 64, AV_K = 16;
 template <class R>
 __global__ void __launch_bounds__(256) k_applyV(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Wb,
                                                 int64_t ldwp, int64_t sWb, C<R> *Eb, int64_t lde, int64_t sE,
-                                                const int *nvec, const int64_t *rng, int k0, int jb) {
+                                                const int *nvec, const int64_t *rng, int k0, int jb, int ncol_fixed) {
   __shared__ C<R> sV[AV_K][AV_T];
   __shared__ C<R> sY[AV_K][AV_T];
   const int b = blockIdx.z;
   const int n = nvec[b];
-  const int m = (int)rng[b * 8 + 2];
+  const int m = ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2];
   const int r0 = k0 + 1 + blockIdx.x * AV_T, c0 = blockIdx.y * AV_T;
   if (r0 >= n || c0 >= m) return;
   const C<R> *A = Ab + b * sA;
@@ -1030,17 +1074,127 @@ cudaError_t back_transform(EigWork &w, cudaStream_t s) {
     const int jb = min(nb, nref - k0);
     const int ks = cdiv(nmax - k0 - 1, BT_RCH);
     // Tf from G = V^H V
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, ldwp, sWp)));
-    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb, sWb)));
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, ldwp, sWp, 0)));
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb, sWb, 0)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
     // Y = Tf V^H E ; E -= V Y
     PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
-                                                             jb, Wp, ldwp, sWp)));
-    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb)));
+                                                             jb, Wp, ldwp, sWp, 0)));
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, 0)));
     PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
-        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb)));
+        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb, 0)));
     count_launch(6);
   }
+  return cudaGetLastError();
+}
+
+// X = P^T (unit columns at the selected rows)
+template <class R>
+__global__ void k_rows_init(C<R> *Xb, int64_t ldx, int64_t sX, const int *rows, int nrows, const int *nvec) {
+  const int b = blockIdx.z;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (r >= nvec[b] || k >= nrows) return;
+  Xb[b * sX + r + ldx * k] = (r == rows[k]) ? cfrom64<R>(1.0, 0.0) : cz<R>();
+}
+
+// Eb(k, j) = sum_r conj(X(r,k)) Z(r,j), Z real (stored as complex with zero
+// imaginary part): the selected rows of E = Q Z.
+constexpr int XZ_T = 64, XZ_K = 16;
+template <class R>
+__global__ void __launch_bounds__(256) k_xhz(const C<R> *Xb, int64_t ldx, int64_t sX, const C<R> *Zb, int64_t ldz,
+                                             int64_t sZ, C<R> *Eb, int64_t lde, int64_t sE, const int *nvec,
+                                             const int64_t *rng, int nrows) {
+  __shared__ C<R> sXt[XZ_K][XZ_T];
+  __shared__ R sZt[XZ_K][XZ_T];
+  const int b = blockIdx.z;
+  const int n = nvec[b];
+  const int m = (int)rng[b * 8 + 2];
+  const int k0 = blockIdx.x * XZ_T, j0 = blockIdx.y * XZ_T;
+  if (k0 >= nrows || j0 >= m) return;
+  const C<R> *X = Xb + b * sX;
+  const C<R> *Z = Zb + b * sZ;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  C<R> acc[4][4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = cz<R>();
+  for (int r0 = 0; r0 < n; r0 += XZ_K) {
+    for (int e = threadIdx.x; e < XZ_K * XZ_T; e += 256) {
+      const int x = e % XZ_T, y = e / XZ_T;
+      const int r = r0 + y;
+      sXt[y][x] = (r < n && k0 + x < nrows) ? cconj(X[r + ldx * (k0 + x)]) : cz<R>();
+      sZt[y][x] = (r < n && j0 + x < m) ? Z[r + ldz * (j0 + x)].re : RT<R>::zero();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int y = 0; y < XZ_K; ++y) {
+      C<R> xv[4];
+      R zv[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        xv[p] = sXt[y][tx + 16 * p];
+        zv[p] = sZt[y][ty + 16 * p];
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          RT<R>::mac(acc[p][q].re, xv[p].re, zv[q]);
+          RT<R>::mac(acc[p][q].im, xv[p].im, zv[q]);
+        }
+    }
+    __syncthreads();
+  }
+  C<R> *E = Eb + b * sE;
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + tx + 16 * p, j = j0 + ty + 16 * q;
+      if (k < nrows && j < m) E[k + lde * j] = cfin(acc[p][q]);
+    }
+}
+
+template <class R>
+cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaStream_t s) {
+  const int B = w.B, nmax = w.nmax, nb = w.nb;
+  if (nrows <= 0) return cudaSuccess;
+  const int64_t ldx = w.lda, sX = (int64_t)w.lda * w.nbr;
+  C<R> *A = (C<R> *)w.A;
+  C<R> *X = (C<R> *)w.Xr;
+  C<R> *Wp = (C<R> *)w.Wp;
+  C<R> *Wb = (C<R> *)w.Wb;
+  const int64_t ldwp = w.ldwp;
+  const int64_t sWp = (int64_t)w.ksplit * 32 * ldwp;
+  const int64_t sWb = (int64_t)32 * ldwp;
+  const int64_t sd = w.nmax;
+  k_rows_init<R><<<dim3(cdiv(nmax, 256), nrows, B), 256, 0, s>>>(X, ldx, sX, d_rows, nrows, w.nvec);
+  count_launch(1);
+  // X <- Q^H X = Q_last^H ... Q_0^H X: panels in forward order, Tf^H
+  const int nref = nmax - 1;
+  for (int k0 = 0; k0 < nref; k0 += nb) {
+    const int jb = min(nb, nref - k0);
+    const int ks = cdiv(nmax - k0 - 1, BT_RCH);
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb,
+                                                            Wp, ldwp, sWp, 0)));
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb,
+                                                            sWb, 0)));
+    k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(nrows, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, X, ldx, sX, 0, w.nvec,
+                                                                             w.rng, k0, jb, Wp, ldwp, sWp, nrows)));
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(nrows, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 2,
+                                                                          w.G, w.Tf, Wb, sWb, nrows)));
+    PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(
+                            A, w.lda, w.sA, Wb, ldwp, sWb, X, ldx, sX, w.nvec, w.rng, k0, jb, nrows)));
+    count_launch(6);
+  }
+  // Eb = X^H Z
+  PP_KT(KT_XHZ, s, (k_xhz<R><<<dim3(cdiv(nrows, XZ_T), cdiv(w.mcap, XZ_T), B), 256, 0, s>>>(
+                       X, ldx, sX, (const C<R> *)w.E, w.lde, w.sE, (C<R> *)w.Eb, (int64_t)w.nbr,
+                       (int64_t)w.nbr * w.mcap, w.nvec, w.rng, nrows)));
+  count_launch(1);
   return cudaGetLastError();
 }
 
@@ -1051,5 +1205,7 @@ template cudaError_t tridiag_eigenvectors<double>(EigWork &, cudaStream_t);
 template cudaError_t tridiag_eigenvectors<df>(EigWork &, cudaStream_t);
 template cudaError_t back_transform<double>(EigWork &, cudaStream_t);
 template cudaError_t back_transform<df>(EigWork &, cudaStream_t);
+template cudaError_t back_transform_rows<double>(EigWork &, const int *, int, cudaStream_t);
+template cudaError_t back_transform_rows<df>(EigWork &, const int *, int, cudaStream_t);
 
 }  // namespace pp

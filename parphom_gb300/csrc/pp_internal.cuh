@@ -16,7 +16,7 @@ void count_launch(int64_t k = 1);
 // (pp_ktimer_enable / pp_ktimer_report).
 enum KClass {
   KT_ASSEMBLE = 0, KT_COLUPD, KT_REFL, KT_HEMV, KT_DOTS, KT_WCORR, KT_WFIN, KT_HER2K, KT_BISECT, KT_INVIT,
-  KT_VHX, KT_BTRED, KT_APPLYV, KT_VEL, KT_N
+  KT_VHX, KT_BTRED, KT_APPLYV, KT_VEL, KT_XHZ, KT_N
 };
 extern unsigned kt_mask;
 void kt_begin(int k, cudaStream_t s);
@@ -75,6 +75,11 @@ struct EigWork {
   int ksplit = 0;
   int ldwp = 0;
 
+  // velocities-only back-transform: boundary rows of E (see back_transform_rows)
+  void *Xr = nullptr;     // [B][nmax*nbr]  Q^H P^T
+  void *Eb = nullptr;     // [B][nbr*mcap]  rows of E = Q Z
+  int nbr = 0;
+
   size_t bytes = 0;
 };
 
@@ -92,6 +97,9 @@ struct Geometry {
   int64_t nbnd = 0;             // boundary blocks (I<J, non-home image, Phi != 0)
   int2 *d_bnd = nullptr;        // [nbnd] (I, J)
   uint16_t *d_bndmask = nullptr;// [nbnd]
+  int64_t nbrows = 0;           // rows of atoms that appear in boundary blocks
+  int *d_brows = nullptr;       // [nbrows] sorted row indices
+  int *d_rowmap = nullptr;      // [n] compact index of a boundary row, -1 otherwise
 };
 
 // ---- kernels launched from pp_capi.cu -------------------------------------
@@ -107,9 +115,11 @@ cudaError_t assemble_deriv(const Geometry &g, const double *d_q, int derivative,
                            int64_t ldo, cudaStream_t s);
 
 // Group velocities: vel[b][3][m] (raw Re e^H dD e), E in 16-byte storage.
+// With rowmap != nullptr, E holds only the boundary rows (row r of the full
+// matrix at E[rowmap[r] + lde*j]).
 cudaError_t velocities(const Geometry &g, const double *d_q, int B, const void *E, int64_t lde, int64_t sE,
                        int efmt, const int64_t *d_rng, int mmax, char method, double *d_vraw, double *d_part,
-                       int nsplit, cudaStream_t s);
+                       int nsplit, const int *rowmap, cudaStream_t s);
 
 // G(r,c) += Re(M(c,r) p(r,c)), M = Z diag(wgt) Z^H for one q (FP64 Z, m columns).
 cudaError_t backward_phi(const Geometry &g, const double *d_q, const z64 *Z, int64_t ldz, int m, const double *wgt,
@@ -124,6 +134,9 @@ template <class R>
 cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s);
 template <class R>
 cudaError_t back_transform(EigWork &w, cudaStream_t s);
+// Rows `rows` of E = Q Z only: X = Q^H P^T (P selects the rows), Eb = X^H Z.
+template <class R>
+cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaStream_t s);
 
 // Output conversion
 cudaError_t finalize_outputs(EigWork &w, int efmt, int raw_lambda, const double *d_vraw, int want_vel, int want_z,

@@ -132,3 +132,23 @@ def test_errors(cell148):
     with pytest.raises(api.PPError) as e:
         api.PhononContext.from_cell(c, phi)
     assert e.value.code == 1003
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_velocities_without_vectors(cell148, prec):
+    """Velocities when no eigenvectors are returned use only the eigenvector
+    rows of atoms in boundary blocks (Q^H P^T, then X^H Z); same results."""
+    S, ctx = cell148
+    qs = synth.random_qpoints(3, seed=9)
+    for rng, il, iu in (("A", 1, 1), ("I", 40, 200)):
+        opts = api.EigOpts(jobz="N", range=rng, il=il, iu=iu, vel=True, vel_method="A", precision=prec)
+        res = ctx.solve(qs, opts, want_z=False)
+        full = ctx.solve(qs, opts, want_z=True)
+        for t, q in enumerate(qs):
+            ref = O.solve_q(S, q, rng=rng, il=il, iu=iu, vel=True)
+            m = len(ref["w_cm"])
+            assert res.m[t] == m and res.info[t] == 0
+            Dn = np.abs(np.linalg.eigvalsh(S.dynmat(q))).max()
+            vmax = np.abs(ref["vel"]).max()
+            parity.check_velocities(res.vel[t, :m], ref["vel"], ref["lam"], Dn, vmax)
+            np.testing.assert_allclose(res.vel[t, :m], full.vel[t, :m], rtol=0, atol=1e-7 * vmax)
