@@ -87,6 +87,10 @@ struct pp_ctx {
   double *d_q = nullptr;
   double *d_w = nullptr, *d_z = nullptr, *d_vel = nullptr;
   int64_t *d_m = nullptr, *d_nz = nullptr, *d_info = nullptr;
+  // captured CUDA graph of the last batch configuration
+  cudaGraphExec_t gexec = nullptr;
+  char gkey[160] = {0};
+  int64_t glaunches = 0;  // kernels in the captured graph
 };
 
 namespace {
@@ -153,7 +157,14 @@ void linsolve(const double *x, const double *A, double *u) {
   }
 }
 
+void drop_graph(pp_ctx *c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->gexec = nullptr;
+  c->gkey[0] = 0;
+}
+
 void free_ws(pp_ctx *c) {
+  drop_graph(c);
   if (c->ws) cudaFree(c->ws);
   c->ws = nullptr;
   c->ws_bytes = 0;
@@ -312,6 +323,54 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
                             o->vel_method, c->vraw, c->vpart, c->nsplit, nullptr, s));
     }
   }
+  return PP_OK;
+}
+
+bool graphs_enabled() {
+  const char *e = getenv("PARPHOM_GPU_GRAPHS");
+  return !(e && e[0] == '0');
+}
+
+// run_batch through a captured CUDA graph: the launch sequence depends only on
+// the batch size, the options and the workspace, so it is captured once and
+// replayed (one graph launch instead of ~6 launches per matrix column).
+int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
+  if (!graphs_enabled() || pp::kt_mask) return run_batch(c, B, o, mcap, want_z);
+  char key[160];
+  snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d", c->ws, B, o->precision, o->jobz,
+           o->range, o->vel_method, o->vel, (long long)o->il, (long long)o->iu, o->vl, o->vu, o->abstol,
+           want_z ? 1 : 0);
+  cudaStream_t s = c->stream;
+  if (c->gexec && strcmp(key, c->gkey) == 0) {
+    TRY_CUDA(cudaGraphLaunch(c->gexec, s));
+    pp::count_launch(c->glaunches);
+    return PP_OK;
+  }
+  drop_graph(c);
+  TRY_CUDA(prepare_bisect(c->w.nmax));
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return run_batch(c, B, o, mcap, want_z);
+  }
+  const int64_t l0 = pp::g_launches.load();
+  const int r = run_batch(c, B, o, mcap, want_z);
+  c->glaunches = pp::g_launches.load() - l0;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (r != PP_OK || e != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return run_batch(c, B, o, mcap, want_z);
+  }
+  e = cudaGraphInstantiate(&c->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    c->gexec = nullptr;
+    cudaGetLastError();
+    return run_batch(c, B, o, mcap, want_z);
+  }
+  strncpy(c->gkey, key, sizeof(c->gkey) - 1);
+  TRY_CUDA(cudaGraphLaunch(c->gexec, s));
   return PP_OK;
 }
 
@@ -574,7 +633,7 @@ int pp_solve_batch(pp_ctx *c, const double *q, int64_t ldq, int64_t nq, const pp
     for (int b = 0; b < Bb; ++b)
       for (int k = 0; k < 3; ++k) qh[3 * b + k] = q[(t0 + b) + ldq * k];
     TRY_CUDA(cudaMemcpyAsync(c->d_q, qh.data(), sizeof(double) * 3 * Bb, cudaMemcpyHostToDevice, s));
-    r = run_batch(c, Bb, o, mcap, want_z);
+    r = run_batch_graph(c, Bb, o, mcap, want_z);
     if (r) {
       c->broken = 1;
       return r;
@@ -640,7 +699,18 @@ int pp_solve_batch_device(pp_ctx *c, const double *q_dev, int64_t ldq, int64_t n
   const int B = pick_batch(c, nq, mcap);
   r = ensure_ws(c, B, mcap);
   if (r) return r;
-  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  // A NULL stream means the legacy default stream: the work then runs on the
+  // library's own stream, ordered after and before the legacy stream with
+  // events (so captured graphs stay usable).
+  const bool legacy = stream == nullptr;
+  cudaStream_t s = legacy ? c->stream : (cudaStream_t)stream;
+  if (legacy) {
+    cudaEvent_t ev;
+    TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, cudaStreamLegacy);
+    cudaStreamWaitEvent(c->stream, ev, 0);
+    cudaEventDestroy(ev);
+  }
   cudaStream_t saved = c->stream;
   c->stream = s;
   for (int64_t t0 = 0; t0 < nq; t0 += B) {
@@ -648,7 +718,7 @@ int pp_solve_batch_device(pp_ctx *c, const double *q_dev, int64_t ldq, int64_t n
     for (int k = 0; k < 3; ++k)
       TRY_CUDA(cudaMemcpy2DAsync(c->d_q + k, 3 * sizeof(double), q_dev + t0 + ldq * k, sizeof(double),
                                  sizeof(double), Bb, cudaMemcpyDeviceToDevice, s));
-    r = run_batch(c, Bb, o, mcap, want_z);
+    r = run_batch_graph(c, Bb, o, mcap, want_z);
     if (r) {
       c->stream = saved;
       c->broken = 1;
@@ -665,6 +735,13 @@ int pp_solve_batch_device(pp_ctx *c, const double *q_dev, int64_t ldq, int64_t n
     }
   }
   c->stream = saved;
+  if (legacy) {
+    cudaEvent_t ev;
+    TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, c->stream);
+    cudaStreamWaitEvent(cudaStreamLegacy, ev, 0);
+    cudaEventDestroy(ev);
+  }
   return PP_OK;
 }
 
@@ -682,7 +759,7 @@ int pp_backward_phi(pp_ctx *c, const double *q_dev, int64_t nq, const double *z_
   if (ldwgt < m) return -9;
   if (!g_dev) return -10;
   if (precision != PP_PREC_FP64 && precision != PP_PREC_MIXED) return -11;
-  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the legacy default stream
   for (int64_t t = 0; t < nq; ++t) {
     cudaError_t e = backward_phi(c->g, q_dev + 3 * t, (const z64 *)(z_dev + zstride * t), ldz, (int)m,
                                  wgt_dev + ldwgt * t, g_dev, precision, s);

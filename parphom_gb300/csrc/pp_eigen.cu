@@ -22,6 +22,7 @@
 //     WY form I - V Tf V^H (zlarft forward/columnwise).
 // Stages 1 and 4 are templated on the real arithmetic R: double (plain FP64
 // form) or df (double-float on the FP32 pipes, the mixed form).
+#include <atomic>
 #include <cfloat>
 #include <cstdio>
 
@@ -76,32 +77,64 @@ constexpr int HV_CC = 32;    // hemv tile width = rows per partial-sum slot
 
 // A(i:n,i) -= V(i:n,0:jj) conj(W(i,0:jj))^T + W(i:n,0:jj) conj(V(i,0:jj))^T ;
 // d[i] = Re A(i,i) ; partial sums of |A(r,i)|^2 for r >= i+2.
+// With fin != 0 it first completes the previous panel column jj-1 (the
+// zlatrd step w += alpha v, alpha = -1/2 tau (w^H v), from the partial sums
+// of k_wcorr): rows >= i+1 are written back by the block that owns them;
+// row i, which every block reads, is completed locally and not written (no
+// later kernel reads it).
 template <class R>
 __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
                                                   const int *nvec, int i, int k0, int jj, double *dd, int64_t sd,
-                                                  double *nrm, int nrb) {
+                                                  double *nrm, int nrb, int fin, int nprev, const z64 *scal,
+                                                  const z64 *wv) {
   __shared__ C<R> sv[64], sw[64];
   __shared__ double red[32];
+  __shared__ z64 s_alpha;
   const int b = blockIdx.y;
   const int n = nvec[b];
   if (i >= n) return;
   C<R> *A = Ab + b * sA;
   C<R> *W = Wb + b * sW;
   const int64_t ldw = lda;
+  if (fin && threadIdx.x == 0) {
+    z64 sacc{0.0, 0.0};
+    for (int k = 0; k < nprev; ++k) {
+      sacc.re += wv[b * nrb + k].re;
+      sacc.im += wv[b * nrb + k].im;
+    }
+    const z64 ts = zmul(scal[b * 4 + 1], sacc);
+    s_alpha = z64{-0.5 * ts.re, -0.5 * ts.im};
+  }
+  __syncthreads();
+  const C<R> alpha = fin ? cfrom64<R>(s_alpha) : cz<R>();
   for (int c = threadIdx.x; c < jj; c += blockDim.x) {
     sv[c] = A[i + lda * (k0 + c)];
-    sw[c] = W[i + ldw * c];
+    C<R> wc = W[i + ldw * c];
+    if (fin && c == jj - 1) {
+      C<R> t = wc;
+      cmac(t, alpha, A[i + lda * (i - 1)]);
+      wc = cfin(t);
+    }
+    sw[c] = wc;
   }
   __syncthreads();
   const int r = i + blockIdx.x * TR_NT + threadIdx.x;
   double part = 0.0;
   if (r < n) {
+    C<R> wlast = cz<R>();
+    if (fin) {
+      C<R> t = W[r + ldw * (jj - 1)];
+      cmac(t, alpha, A[r + lda * (i - 1)]);
+      wlast = cfin(t);
+      if (r > i) W[r + ldw * (jj - 1)] = wlast;
+    }
     C<R> a = A[r + lda * i];
     if (jj > 0) {
       C<R> acc = cz<R>();
       for (int c = 0; c < jj; ++c) {
+        const C<R> wrc = (fin && c == jj - 1) ? wlast : W[r + ldw * c];
         cmac(acc, A[r + lda * (k0 + c)], cconj(sw[c]));
-        cmac(acc, W[r + ldw * c], cconj(sv[c]));
+        cmac(acc, wrc, cconj(sv[c]));
       }
       a = csub(a, cfin(acc));
     }
@@ -115,8 +148,8 @@ __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t
       part = t.re * t.re + t.im * t.im;
     }
   }
-  double s = block_sum<TR_NT>(part, red);
-  if (threadIdx.x == 0) nrm[b * nrb + blockIdx.x] = s;
+  double sn = block_sum<TR_NT>(part, red);
+  if (threadIdx.x == 0) nrm[b * nrb + blockIdx.x] = sn;
 }
 
 // zlarfg on A(i+1:n, i); v := [1, x/(alpha-beta)] written back in place.
@@ -437,10 +470,15 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
   const int64_t sd = w.nmax;
   for (int k0 = 0; k0 < nmax; k0 += nb) {
     const int jb = min(nb, nmax - k0);
+    int nprev = 0;  // k_wcorr blocks of the previous column, when its w is still to be completed
     for (int jj = 0; jj < jb; ++jj) {
       const int i = k0 + jj;
       const int nparts = cdiv(nmax - i, TR_NT);
-      PP_KT(KT_COLUPD, s, (k_colupd<R><<<dim3(nparts, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, w.d, sd, w.nrm, w.nrb)));
+      const int fin = (jj > 0 && nprev > 0) ? 1 : 0;
+      PP_KT(KT_COLUPD, s, (k_colupd<R><<<dim3(nparts, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, w.d, sd,
+                                                                         w.nrm, w.nrb, fin, nprev, w.scal,
+                                                                         (z64 *)w.wv)));
+      nprev = 0;
       if (i >= nmax - 1) {
         count_launch(1);
         continue;
@@ -455,8 +493,14 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
       const int nrw = cdiv(m, WC_ROWS);
       PP_KT(KT_WCORR, s, (k_wcorr<R><<<dim3(nrw, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, P, sP, lda, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb,
                                                w.scal, (z64 *)w.wv, w.nrb)));
-      PP_KT(KT_WFIN, s, (k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nrw, w.scal, (z64 *)w.wv, w.nrb)));
-      count_launch(jj > 0 ? 6 : 5);
+      if (jj == jb - 1 || i == nmax - 2) {
+        // last column of the panel: the trailing update reads W next
+        PP_KT(KT_WFIN, s, (k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nrw, w.scal, (z64 *)w.wv, w.nrb)));
+        count_launch(jj > 0 ? 7 : 6);
+      } else {
+        nprev = nrw;  // completed by the next column's k_colupd
+        count_launch(jj > 0 ? 6 : 5);
+      }
     }
     const int k1 = k0 + jb;
     if (k1 < nmax) {
@@ -640,6 +684,21 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
   wout[b * sd + j] = 0.5 * (lo + hi);
 }
 
+// Opt the bisection kernel into the dynamic shared memory it needs for order
+// n (done once per size outside any stream capture).
+cudaError_t prepare_bisect(int n) {
+  static std::atomic<int> done{0};
+  const int need = (int)(2 * (size_t)n * (sizeof(double) + sizeof(float)));
+  if (need <= done.load() || need > 200 * 1024) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
+  if (e == cudaSuccess) {
+    int cur = done.load();
+    while (need > cur && !done.compare_exchange_weak(cur, need)) {
+    }
+  }
+  return e;
+}
+
 cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, int64_t il, int64_t iu, double abstol,
                                 cudaStream_t s) {
   const int64_t sd = w.nmax;
@@ -647,7 +706,7 @@ cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, in
   size_t smem = 2 * (size_t)w.nmax * (sizeof(double) + sizeof(float));
   int use_smem = smem <= 200 * 1024;
   if (use_smem) {
-    PP_CUDA_TRY(cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PP_CUDA_TRY(prepare_bisect(w.nmax));
   } else {
     smem = 0;
   }

@@ -128,6 +128,7 @@ cudaError_t backward_phi(const Geometry &g, const double *d_q, const z64 *Z, int
 // Eigen stages, templated on the real type (double / df) in pp_eigen.cu.
 template <class R>
 cudaError_t tridiagonalize(EigWork &w, cudaStream_t s);
+cudaError_t prepare_bisect(int n);
 cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, int64_t il, int64_t iu,
                                 double abstol, cudaStream_t s);
 template <class R>
