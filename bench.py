@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--batch", type=int, default=4, help="q-points per step and rank")
+    p.add_argument("--batch", type=int, default=16, help="q-points per step and rank")
     p.add_argument("--m", type=int, default=11, help="twist index (11 -> N=1588)")
     p.add_argument("--fp64-batch", type=int, default=0, help="q per FP64-form step (0: same as --batch)")
     p.add_argument("--no-cpu-baseline", action="store_true")

@@ -135,6 +135,17 @@ PP_API int pp_solve_batch(pp_ctx *ctx, const double *q, int64_t ldq, int64_t nq,
 PP_API int pp_solve_batch_device(pp_ctx *ctx, const double *q_dev, int64_t ldq, int64_t nq, const pp_eig_opts *opts,
                           const pp_result_view *out_dev, int64_t *info_dev, void *stream);
 
+/* Several cells (contexts of different sizes) in one launch sequence: q-point
+ * t (q[t + ldq*k]) belongs to cell ctxs[cell[t]].  The q-points are grouped
+ * by cell into batches of mixed orders; assembly and velocities run per cell,
+ * the reduction, bisection, inverse iteration and back-transform once per
+ * batch (every kernel carries each matrix's own order).  Outputs as for
+ * pp_solve_batch with ldw (and ldz) at least the largest 3N; the workspace
+ * belongs to ctxs[0] and is released at the end.  No counterpart in the
+ * reference, which runs one cell per program. */
+PP_API int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const double *q, int64_t ldq,
+                          int64_t nq, const pp_eig_opts *opts, const pp_result_view *out, int64_t *info);
+
 /* D(q) (derivative = 0) or dD/dq_k (derivative = k in 1..3, vel_method 'A'
  * or 'C') for one q, written as the full Hermitian matrix (upper triangle
  * mirrored) to host buffer d[2*(r + ldd*c)].

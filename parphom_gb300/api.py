@@ -31,7 +31,7 @@ INFO_NOTCOMP = 8
 
 EXPORTED = ("pp_ctx_create", "pp_ctx_destroy", "pp_solve_batch", "pp_solve_batch_device", "pp_dynamical_matrix",
             "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report",
-            "pp_heevx_values_noalloc", "pp_backward_phi")
+            "pp_heevx_values_noalloc", "pp_backward_phi", "pp_solve_multi")
 PP_ERR_SIZE = 1008
 PP_NOALLOC_MAX_N = 1536
 
@@ -102,6 +102,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                           ctypes.c_double, _i64, _i64, ctypes.c_double, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.pp_heevx_values_noalloc.restype = ctypes.c_int
+    L.pp_solve_multi.argtypes = [ctypes.POINTER(ctypes.c_void_p), _i64, _ip, _dp, _i64, _i64,
+                                 ctypes.POINTER(PPEigOpts), ctypes.POINTER(PPResultView), _ip]
+    L.pp_solve_multi.restype = ctypes.c_int
     L.pp_backward_phi.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _i64, ctypes.c_void_p, _i64, _i64, _i64,
                                   ctypes.c_void_p, _i64, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
     L.pp_backward_phi.restype = ctypes.c_int
@@ -261,6 +264,40 @@ class PhononContext:
                                              ctypes.c_void_p(int(stream)))
         if rc != 0:
             raise PPError(rc, "pp_solve_batch_device")
+
+
+def solve_multi(contexts, cell, q, opts: EigOpts | None = None, want_z: bool = True) -> Result:
+    """pp_solve_multi: q-points of several cells (`cell[t]` indexes
+    `contexts`) solved in shared batches of mixed matrix orders.  Arrays are
+    sized for the largest cell (n_max); entries beyond a cell's own 3N are
+    unset."""
+    opts = opts or EigOpts()
+    L = load()
+    q = np.atleast_2d(np.asarray(q, np.float64))
+    nq = q.shape[0]
+    cell = np.ascontiguousarray(cell, np.int64)
+    nmax = max(c.n for c in contexts)
+    qf = np.asfortranarray(q)
+    m = np.zeros(nq, np.int64)
+    nz = np.zeros(nq, np.int64)
+    info = np.zeros(nq, np.int64)
+    w = np.zeros((nq, nmax))
+    vecs = opts.jobz == "V" or opts.vel
+    z = np.zeros((nq, nmax, nmax), np.complex128) if (vecs and want_z) else None
+    vel = np.zeros((nq, nmax, 3)) if opts.vel else None
+    zv = z.view(np.float64) if z is not None else None
+    rv = PPResultView(m.ctypes.data_as(_ip), nz.ctypes.data_as(_ip), _p(w), nmax,
+                      _p(zv) if zv is not None else None, nmax, 2 * nmax * nmax,
+                      _p(vel) if vel is not None else None, 3 * nmax, None)
+    handles = (ctypes.c_void_p * len(contexts))(*[c._h.value for c in contexts])
+    oc = opts.to_c()
+    rc = L.pp_solve_multi(handles, len(contexts), cell.ctypes.data_as(_ip), qf.ctypes.data_as(_dp), nq, nq,
+                          ctypes.byref(oc), ctypes.byref(rv), info.ctypes.data_as(_ip))
+    if rc != 0:
+        raise PPError(rc, "pp_solve_multi")
+    if z is not None:
+        z = np.ascontiguousarray(z.transpose(0, 2, 1))
+    return Result(m=m, nz=nz, w=w, z=z, vel=vel, info=info)
 
 
 def heevx_values_noalloc(a_ptr: int, lda: int, n: int, w_ptr: int, m_ptr: int, info_ptr: int, range: str = "A",

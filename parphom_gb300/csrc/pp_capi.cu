@@ -1,6 +1,7 @@
 // C ABI of the phonon hot path: context lifetime, workspace sizing and the
 // per-batch pipeline  D(q) -> tridiagonal -> eigenvalues -> eigenvectors ->
 // back-transform -> velocities -> outputs.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdlib>
@@ -76,6 +77,7 @@ struct pp_ctx {
   // workspace (grown on demand)
   EigWork w;
   int cap_B = 0, cap_m = 0;
+  int64_t cap_n = 0, cap_nbnd = 0, cap_nbr = 0;
   int cap_prec = -1;
   void *ws = nullptr;
   size_t ws_bytes = 0;
@@ -169,25 +171,27 @@ void free_ws(pp_ctx *c) {
   c->ws = nullptr;
   c->ws_bytes = 0;
   c->cap_B = c->cap_m = 0;
+  c->cap_n = c->cap_nbnd = c->cap_nbr = 0;
   c->w = EigWork();
 }
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Carve every batch buffer out of one allocation.
-int ensure_ws(pp_ctx *c, int B, int mcap) {
-  if (c->ws && B <= c->cap_B && mcap <= c->cap_m) return PP_OK;
+int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int64_t nbr_max) {
+  if (c->ws && B <= c->cap_B && mcap <= c->cap_m && n == c->cap_n && nbnd_max <= c->cap_nbnd &&
+      nbr_max == c->cap_nbr)
+    return PP_OK;
   free_ws(c);
-  const int64_t n = c->g.n;
   const int nb = 32;
   const int64_t lda = (n + 7) / 8 * 8;
   const int nchunk = (int)((n + 31) / 32);
   const int nrb = (int)((n + 31) / 32) + 1;  // partial sums per column kernel block
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
-  const int nbr = (int)c->g.nbrows;
+  const int nbr = (int)nbr_max;
   const int ldwp = std::max(std::max(mcap, nbr), 64);
   const int ksplit = (int)((n + 511) / 512);
-  const int64_t nbnd = c->g.nbnd;
+  const int64_t nbnd = nbnd_max;
   std::vector<std::pair<void **, size_t>> parts;
   EigWork &w = c->w;
   w = EigWork();
@@ -256,10 +260,15 @@ int ensure_ws(pp_ctx *c, int B, int mcap) {
   w.bytes = off;
   c->cap_B = B;
   c->cap_m = mcap;
+  c->cap_n = n;
+  c->cap_nbnd = nbnd_max;
+  c->cap_nbr = nbr_max;
   std::vector<int> nv(B, (int)n);
   TRY_CUDA(cudaMemcpy(w.nvec, nv.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
   return PP_OK;
 }
+
+int ensure_ws(pp_ctx *c, int B, int mcap) { return ensure_ws_sized(c, B, mcap, c->g.n, c->g.nbnd, c->g.nbrows); }
 
 size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd, int64_t nbr) {
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
@@ -284,6 +293,45 @@ int check_opts(const pp_ctx *c, const pp_eig_opts *o) {
 
 // Run the pipeline for B q-points already in c->d_q; results left in the
 // EigWork buffers, velocities in c->vraw.
+// The matrices [off, off+cnt) of a batch as a batch of their own (every
+// per-matrix buffer shifted by `off` of its per-matrix stride).
+EigWork view_of(const EigWork &w, int off, int cnt) {
+  EigWork v = w;
+  v.B = cnt;
+  auto sh = [off](void *p, size_t stride_bytes) -> void * {
+    return p ? (void *)((char *)p + stride_bytes * (size_t)off) : nullptr;
+  };
+  const size_t nmax = (size_t)w.nmax;
+  const int64_t T = w.scratch_threads;
+  v.nvec = w.nvec + off;
+  v.A = sh(w.A, 16 * (size_t)w.sA);
+  v.E = sh(w.E, 16 * (size_t)w.sE);
+  v.W = sh(w.W, 16 * (size_t)w.lda * w.nb);
+  v.P = sh(w.P, 16 * (size_t)w.nchunk * w.lda);
+  v.X = sh(w.X, 16 * 2 * (size_t)w.nb);
+  v.nrm = (double *)sh(w.nrm, 8 * (size_t)w.nrb);
+  v.wv = (z64 *)sh(w.wv, 16 * (size_t)w.nrb);
+  v.d = (double *)sh(w.d, 8 * nmax);
+  v.e = (double *)sh(w.e, 8 * nmax);
+  v.tau = (z64 *)sh(w.tau, 16 * nmax);
+  v.scal = (z64 *)sh(w.scal, 16 * 4);
+  v.w = (double *)sh(w.w, 8 * nmax);
+  v.rng = (int64_t *)sh(w.rng, 8 * 8);
+  v.tinfo = (double *)sh(w.tinfo, 8 * 8);
+  v.cls = (int *)sh(w.cls, 4 * (nmax + 1));
+  v.ncl = (int *)sh(w.ncl, 4);
+  v.scratch = (double *)sh(w.scratch, 8 * 5 * nmax * (size_t)T);
+  v.piv = (uint8_t *)sh(w.piv, nmax * (size_t)T);
+  v.info = (int64_t *)sh(w.info, 8);
+  v.Tf = (z64 *)sh(w.Tf, 16 * 1024);
+  v.G = (z64 *)sh(w.G, 16 * 1024);
+  v.Wb = sh(w.Wb, 16 * 32 * (size_t)w.ldwp);
+  v.Wp = sh(w.Wp, 16 * (size_t)w.ksplit * 32 * w.ldwp);
+  v.Xr = sh(w.Xr, 16 * (size_t)w.lda * std::max(w.nbr, 1));
+  v.Eb = sh(w.Eb, 16 * (size_t)std::max(w.nbr, 1) * w.mcap);
+  return v;
+}
+
 int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   EigWork &w = c->w;
   w.B = B;
@@ -794,6 +842,159 @@ int pp_dynamical_matrix(pp_ctx *c, const double *q, int64_t derivative, char vel
   cudaFree(dq);
   cudaFree(dout);
   return cuda_err(e);
+}
+
+
+int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const double *q, int64_t ldq, int64_t nq,
+                   const pp_eig_opts *o, const pp_result_view *out, int64_t *info) {
+  if (!ctxs || nctx < 1) return -1;
+  if (!cell && nq > 0) return -3;
+  if (!q && nq > 0) return -4;
+  if (ldq < nq) return -5;
+  if (nq < 0) return -6;
+  if (!out || !out->w || !out->m || !out->nz) return -8;
+  int64_t nmax = 0, nbnd = 0, nbr = 0;
+  for (int64_t k = 0; k < nctx; ++k) {
+    if (!ctxs[k]) return -1;
+    if (ctxs[k]->broken) return PP_ERR_STATE;
+    const int r = check_opts(ctxs[k], o);
+    if (r) return r == -5 ? -7 : r;
+    nmax = std::max(nmax, ctxs[k]->g.n);
+    nbnd = std::max(nbnd, ctxs[k]->g.nbnd);
+    nbr = std::max(nbr, ctxs[k]->g.nbrows);
+  }
+  if (nq == 0) return PP_OK;
+  for (int64_t t = 0; t < nq; ++t) {
+    if (cell[t] < 0 || cell[t] >= nctx) return -3;
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(q[t + ldq * k])) return PP_ERR_NAN;
+  }
+  if (out->ldw < nmax) return -8;
+  const bool vecs = o->jobz == 'V' || o->vel;
+  const bool want_z = vecs && out->z;
+  if (want_z && out->ldz < nmax) return -8;
+  bool rows_only = o->vel && !want_z;
+  for (int64_t k = 0; k < nctx; ++k) rows_only = rows_only && ctxs[k]->g.nbrows < ctxs[k]->g.n;
+  pp_ctx *h = ctxs[0];
+  const int mcap = o->range == 'I' ? (int)(o->iu - o->il + 1) : (int)nmax;
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  if (h->ws) fr += h->ws_bytes;
+  int B = (int)std::min<int64_t>(nq, 64);
+  while (B > 1 && ws_bytes_estimate(nmax, B, mcap, nbnd, nbr) > (size_t)(0.6 * (double)fr)) B /= 2;
+  if (const char *env = getenv("PARPHOM_GPU_BATCH")) {
+    const int v = atoi(env);
+    if (v > 0) B = (int)std::min<int64_t>(v, nq);
+  }
+  int r = ensure_ws_sized(h, B, mcap, nmax, nbnd, nbr);
+  if (r) return r;
+  EigWork &w = h->w;
+  cudaStream_t s = h->stream;
+  const int prec = o->precision;
+  const int fmt = prec == PP_PREC_MIXED ? 1 : 0;
+  // q-points grouped by cell, so that every cell's matrices are adjacent
+  std::vector<int64_t> order(nq);
+  for (int64_t t = 0; t < nq; ++t) order[t] = t;
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cell[a] < cell[b]; });
+  std::vector<double> qh(3 * (size_t)B);
+  std::vector<int> nv(B);
+  std::vector<int64_t> mh(B), nzh(B), infoh(B);
+  for (int64_t t0 = 0; t0 < nq; t0 += B) {
+    const int Bb = (int)std::min<int64_t>(B, nq - t0);
+    struct Seg {
+      pp_ctx *c;
+      int off, cnt;
+    };
+    std::vector<Seg> segs;
+    for (int b = 0; b < Bb; ++b) {
+      const int64_t t = order[t0 + b];
+      pp_ctx *c = ctxs[cell[t]];
+      for (int k = 0; k < 3; ++k) qh[3 * b + k] = q[t + ldq * k];
+      nv[b] = (int)c->g.n;
+      if (segs.empty() || segs.back().c != c)
+        segs.push_back({c, b, 1});
+      else
+        segs.back().cnt++;
+    }
+    TRY_CUDA(cudaMemcpyAsync(h->d_q, qh.data(), sizeof(double) * 3 * Bb, cudaMemcpyHostToDevice, s));
+    TRY_CUDA(cudaMemcpyAsync(w.nvec, nv.data(), sizeof(int) * Bb, cudaMemcpyHostToDevice, s));
+    w.B = Bb;
+    for (auto &g : segs) {
+      EigWork v = view_of(w, g.off, g.cnt);
+      TRY_CUDA(assemble_batch(g.c->g, h->d_q + 3 * g.off, g.cnt, v.A, w.lda, w.sA, fmt, s));
+    }
+    if (prec == PP_PREC_MIXED)
+      TRY_CUDA(tridiagonalize<df>(w, s));
+    else
+      TRY_CUDA(tridiagonalize<double>(w, s));
+    TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s));
+    if (vecs) {
+      if (prec == PP_PREC_MIXED)
+        TRY_CUDA(tridiag_eigenvectors<df>(w, s));
+      else
+        TRY_CUDA(tridiag_eigenvectors<double>(w, s));
+      if (!rows_only) {
+        if (prec == PP_PREC_MIXED)
+          TRY_CUDA(back_transform<df>(w, s));
+        else
+          TRY_CUDA(back_transform<double>(w, s));
+      }
+      for (auto &g : segs) {
+        EigWork v = view_of(w, g.off, g.cnt);
+        if (rows_only) {
+          if (prec == PP_PREC_MIXED)
+            TRY_CUDA(back_transform_rows<df>(v, g.c->g.d_brows, (int)g.c->g.nbrows, s));
+          else
+            TRY_CUDA(back_transform_rows<double>(v, g.c->g.d_brows, (int)g.c->g.nbrows, s));
+        }
+        if (o->vel) {
+          double *vr = h->vraw + (size_t)g.off * 3 * w.mcap;
+          if (rows_only)
+            TRY_CUDA(velocities(g.c->g, h->d_q + 3 * g.off, g.cnt, v.Eb, w.nbr, (int64_t)w.nbr * w.mcap, fmt, v.rng,
+                                w.mcap, o->vel_method, vr, h->vpart, h->nsplit, g.c->g.d_rowmap, s));
+          else
+            TRY_CUDA(velocities(g.c->g, h->d_q + 3 * g.off, g.cnt, v.E, w.lde, w.sE, fmt, v.rng, w.mcap,
+                                o->vel_method, vr, h->vpart, h->nsplit, nullptr, s));
+        }
+      }
+    }
+    TRY_CUDA(finalize_outputs(w, fmt, o->raw_lambda, h->vraw, o->vel ? 1 : 0, 0, h->d_w, nmax, nullptr, 0, 0, h->d_vel,
+                              3 * (int64_t)w.mcap, h->d_m, h->d_nz, h->d_info, vecs ? 1 : 0, s));
+    TRY_CUDA(cudaMemcpyAsync(mh.data(), h->d_m, 8 * Bb, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaMemcpyAsync(nzh.data(), h->d_nz, 8 * Bb, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaMemcpyAsync(infoh.data(), h->d_info, 8 * Bb, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaStreamSynchronize(s));
+    for (int b = 0; b < Bb; ++b) {
+      const int64_t t = order[t0 + b];
+      out->m[t] = mh[b];
+      out->nz[t] = vecs ? nzh[b] : 0;
+      if (info) info[t] = infoh[b];
+      if (mh[b] > 0) {
+        TRY_CUDA(cudaMemcpyAsync(out->w + out->ldw * t, h->d_w + nmax * b, sizeof(double) * mh[b],
+                                 cudaMemcpyDeviceToHost, s));
+        if (o->vel && out->vel)
+          TRY_CUDA(cudaMemcpyAsync(out->vel + out->velstride * t, h->d_vel + 3 * (int64_t)w.mcap * b,
+                                   sizeof(double) * 3 * mh[b], cudaMemcpyDeviceToHost, s));
+      }
+    }
+    if (want_z) {
+      double *zst = (double *)w.A;
+      TRY_CUDA(finalize_outputs(w, fmt, o->raw_lambda, h->vraw, 0, 1, nullptr, 0, zst, w.lda, 2 * w.sA, nullptr, 0,
+                                nullptr, nullptr, nullptr, 1, s));
+      for (int b = 0; b < Bb; ++b) {
+        const int64_t t = order[t0 + b];
+        if (mh[b] > 0)
+          TRY_CUDA(cudaMemcpy2DAsync(out->z + out->zstride * t, sizeof(double) * 2 * out->ldz, zst + 2 * w.sA * b,
+                                     sizeof(double) * 2 * w.lda, sizeof(double) * 2 * nv[b], mh[b],
+                                     cudaMemcpyDeviceToHost, s));
+      }
+    }
+    TRY_CUDA(cudaStreamSynchronize(s));
+  }
+  // the workspace was sized for the largest cell: release it, the next
+  // single-cell call sizes its own
+  free_ws(h);
+  return PP_OK;
 }
 
 }  // extern "C"

@@ -152,3 +152,35 @@ def test_velocities_without_vectors(cell148, prec):
             vmax = np.abs(ref["vel"]).max()
             parity.check_velocities(res.vel[t, :m], ref["vel"], ref["lam"], Dn, vmax)
             np.testing.assert_allclose(res.vel[t, :m], full.vel[t, :m], rtol=0, atol=1e-7 * vmax)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_uneven_cells_one_batch(tblg28, cell148, prec):
+    """pp_solve_multi: q-points of three cells of different size (N = 28,
+    148, 364) interleaved, solved in shared batches; each result must equal
+    the single-cell solve of the same q."""
+    S28, ctx28, _ = tblg28
+    S148, ctx148 = cell148
+    c364 = synth.tblg_cell(5)
+    phi364 = synth.spring_force_constants(c364, seed=0)
+    ctx364 = api.PhononContext.from_cell(c364, phi364)
+    ctxs = [ctx28, ctx148, ctx364]
+    rng = np.random.default_rng(12)
+    cell = rng.integers(0, 3, 9)
+    q = synth.random_qpoints(9, seed=13)
+    for want_z in (False, True):
+        opts = api.EigOpts(jobz="V" if want_z else "N", vel=True, vel_method="A", precision=prec)
+        res = api.solve_multi(ctxs, cell, q, opts, want_z=want_z)
+        for t in range(9):
+            c = ctxs[cell[t]]
+            single = c.solve(q[t:t + 1], opts, want_z=want_z)
+            n = c.n
+            assert res.m[t] == n and res.info[t] == 0
+            np.testing.assert_allclose(res.w[t, :n], single.w[0, :n], rtol=1e-12, atol=1e-9)
+            vmax = np.abs(single.vel[0, :n]).max()
+            np.testing.assert_allclose(res.vel[t, :n], single.vel[0, :n], rtol=0, atol=1e-9 * vmax)
+            if want_z:
+                Z, Zs = res.z[t][:n, :n], single.z[0][:, :n]
+                ov = np.abs(np.einsum("ij,ij->j", Z.conj(), Zs))
+                assert np.abs(ov - 1).max() < 1e-9
+    ctx364.close()
