@@ -146,6 +146,24 @@ PP_API int pp_solve_batch_device(pp_ctx *ctx, const double *q_dev, int64_t ldq, 
 PP_API int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const double *q, int64_t ldq,
                           int64_t nq, const pp_eig_opts *opts, const pp_result_view *out, int64_t *info);
 
+/* Density of states by linear triangulation (Utilities/pyphutil/
+ * fortran_routines/bz_integration.f90:12-133, called from
+ * pyphutil.py:214-322): freq[k*ldf + b] is band b at grid point k (cm^-1),
+ * func the same layout (NULL: all ones), tri[3*j + v] the vertices of
+ * triangle j.  dos[i] and nd[i] receive the sums over triangles and bands of
+ * the per-triangle contributions at energy[i] (unnormalised, as the Fortran
+ * routine returns them).  Host buffers. */
+PP_API int pp_dos_triangulation(const double *freq, int64_t ldf, int64_t nk, int64_t nbands, const double *func,
+                                const int64_t *tri, int64_t ntri, const double *energy, int64_t ne, double *dos,
+                                double *nd);
+
+/* Gaussian (method 1) or Lorentzian (method 2) smearing DOS
+ * (bz_integration.f90:154-199): dos[i] = sum_q weights[q] sum_b
+ * g(freq[q*ldf+b], energy[i], width) / natom.  Host buffers. */
+PP_API int pp_dos_smearing(int32_t method, const double *freq, int64_t ldf, int64_t nq, int64_t nbands,
+                           const double *weights, double width, const double *energy, int64_t ne, int64_t natom,
+                           double *dos);
+
 /* D(q) (derivative = 0) or dD/dq_k (derivative = k in 1..3, vel_method 'A'
  * or 'C') for one q, written as the full Hermitian matrix (upper triangle
  * mirrored) to host buffer d[2*(r + ldd*c)].
