@@ -197,15 +197,33 @@ def spring_force_constants(cell: Cell, seed: int = 0, noise: float = 0.01,
     rhat = vec / d[:, None]
     K = kval[:, None, None] * ((1.0 - TRANSVERSE) * rhat[:, :, None] * rhat[:, None, :]
                                + TRANSVERSE * np.eye(3)[None])
-    blocks = np.zeros((N, N, 3, 3))
-    np.add.at(blocks, (I, J), -K)
-    blocks = 0.5 * (blocks + blocks.transpose(1, 0, 3, 2))
+    # Phi is filled in its (3N x 3N) layout and symmetrised in place tile by
+    # tile, so that the N = 11164 cell needs one 9 GB matrix and no copies.
+    n = 3 * N
+    phi = np.zeros((n, n))
+    a = np.arange(3)
+    rows = (3 * I)[:, None, None] + a[None, :, None]
+    cols = (3 * J)[:, None, None] + a[None, None, :]
+    np.add.at(phi.reshape(-1), (rows * n + cols).ravel(), -K.ravel())
+    _symmetrize_inplace(phi)
+    blocks = phi.reshape(N, 3, N, 3)
     idx = np.arange(N)
-    blocks[idx, idx] = 0.0
-    blocks[idx, idx] = -blocks.sum(axis=1)
-    phi = blocks.transpose(0, 2, 1, 3).reshape(3 * N, 3 * N)
-    phi = 0.5 * (phi + phi.T)
-    return np.ascontiguousarray(phi)
+    blocks[idx, :, idx, :] = 0.0
+    blocks[idx, :, idx, :] = -blocks.sum(axis=2)
+    _symmetrize_inplace(phi)
+    return phi
+
+
+def _symmetrize_inplace(a: np.ndarray, tile: int = 2048) -> None:
+    """a <- (a + a^T) / 2 without a second n x n array."""
+    n = a.shape[0]
+    for i0 in range(0, n, tile):
+        i1 = min(n, i0 + tile)
+        for j0 in range(i0, n, tile):
+            j1 = min(n, j0 + tile)
+            s = 0.5 * (a[i0:i1, j0:j1] + a[j0:j1, i0:i1].T)
+            a[i0:i1, j0:j1] = s
+            a[j0:j1, i0:i1] = s.T
 
 
 def phi_to_dataset(phi: np.ndarray) -> np.ndarray:
