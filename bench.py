@@ -293,6 +293,12 @@ def main():
         torch.distributed.destroy_process_group()
 
 
+# DRAM bytes (read + write) over algorithmic bytes of one k_hemv_lower launch,
+# measured with ncu --set full at N=1588, batch 4, column 300: 682.6 MB for
+# 637.5 MB (the partial sums written for the w-completion are the 7%).
+HEMV_TRAFFIC_RATIO = 1.071
+
+
 def roofline_for(kclass, rec, n, nq):
     """Algorithmic work of the dominant kernel class over the timed region."""
     launches, ms = rec
@@ -310,7 +316,10 @@ def roofline_for(kclass, rec, n, nq):
         ach = byts / (ms / 1e3) / 1e9
         return {"bound": "hbm", "kernel": "k_hemv_lower (double-float Hermitian mat-vec, lower triangle)",
                 "achieved": ach, "peak": hbm,
-                "unit": "GB/s", "frac": ach / hbm, "peak_source": src, "traffic": None,
+                "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
+                "traffic": HEMV_TRAFFIC_RATIO * byts / launches,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (column 300, "
+                                  "batch 4) = 1.071 x its algorithmic bytes, scaled to this average launch",
                 "launches": launches, "avg_launch_ms": ms / launches,
                 "algorithmic_bytes_per_launch": byts / launches}
     # FP32-pipe kernels (double-float arithmetic): count complex MACs
