@@ -190,7 +190,9 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
   const int nbr = (int)nbr_max;
   const int ldwp = std::max(std::max(mcap, nbr), 64);
-  const int ksplit = (int)((n + 511) / 512);
+  // split-K partials: ceil(n/512) chunks of 32 x ldwp, or the Gram product's
+  // ceil(n/64) chunks of 32 x 32, whichever is larger
+  const int ksplit = (int)std::max<int64_t>((n + 511) / 512, ((n + 63) / 64 * 32 + ldwp - 1) / ldwp);
   const int64_t nbnd = nbnd_max;
   std::vector<std::pair<void **, size_t>> parts;
   EigWork &w = c->w;
@@ -274,6 +276,7 @@ size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd, int64_t nbr) 
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
   size_t per = 16 * (size_t)n * n + 16 * (size_t)n * mcap + 8 * (size_t)5 * n * T + (size_t)n * T +
                16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
+               16 * (size_t)((n + 63) / 64) * 32 * 32 +
                8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd + 16 * (size_t)nbr * (n + mcap);
   return per * B;
 }
@@ -343,7 +346,8 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
     TRY_CUDA(tridiagonalize<df>(w, s));
   else
     TRY_CUDA(tridiagonalize<double>(w, s));
-  TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s));
+  TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s,
+                               prec == PP_PREC_MIXED));
   (void)mcap;
   if (vecs) {
     // Velocities without eigenvector output need only the eigenvector rows
@@ -395,7 +399,7 @@ int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_
     return PP_OK;
   }
   drop_graph(c);
-  TRY_CUDA(prepare_bisect(c->w.nmax));
+  TRY_CUDA(prepare_bisect(bisect_smem(c->w.nmax, o->precision == PP_PREC_MIXED)));
   if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
     cudaGetLastError();
     return run_batch(c, B, o, mcap, want_z);
@@ -927,7 +931,8 @@ int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const
       TRY_CUDA(tridiagonalize<df>(w, s));
     else
       TRY_CUDA(tridiagonalize<double>(w, s));
-    TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s));
+    TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s,
+                                 prec == PP_PREC_MIXED));
     if (vecs) {
       if (prec == PP_PREC_MIXED)
         TRY_CUDA(tridiag_eigenvectors<df>(w, s));

@@ -601,14 +601,62 @@ __device__ __forceinline__ int sturm_count32(const float *d, const float *e2, in
   return c;
 }
 
-// One thread per wanted eigenvalue.  With the tridiagonal in shared memory
-// the interval is first narrowed with FP32 Sturm counts (cheap on the FP32
-// pipes), then widened by a margin far above the FP32 backward error of the
-// count (64 eps32 (||T|| + |x|)), checked with two FP64 counts (falling back to
-// the Gerschgorin interval if the check fails) and finished in FP64.
+// Sturm count in double-float: q_k = (d_k - x) - e2_{k-1} / q_{k-1} with
+// d, e2 and x as hi + lo float pairs.  The quotient is a float estimate
+// corrected once by its exact remainder (TwoProd by FMA), about 44 bits; the
+// count is then exact for a tridiagonal perturbed by a few 2^-44 relative in
+// each entry, the double-float analogue of the FP64 count's backward error.
+__device__ __forceinline__ int sturm_count_df(const float *dh, const float *dl, const float *eh, const float *el,
+                                              int n, df x, float pivmin) {
+  float qh, ql;
+  {
+    float s, e;
+    two_sum(dh[0], -x.hi, s, e);
+    e = __fadd_rn(e, __fsub_rn(dl[0], x.lo));
+    fast_two_sum(s, e, qh, ql);
+  }
+  if (fabsf(qh) <= pivmin) {
+    qh = -pivmin;
+    ql = 0.0f;
+  }
+  int c = qh < 0.0f;
+  for (int k = 1; k < n; ++k) {
+    // t = e2 / q
+    const float a = eh[k - 1], al = el[k - 1];
+    const float th = __fdividef(a, qh);
+    const float p = __fmul_rn(th, qh);
+    const float pe = __fmaf_rn(th, qh, -p);
+    float rem = __fsub_rn(a, p);
+    rem = __fsub_rn(rem, pe);
+    rem = __fadd_rn(rem, al);
+    rem = __fmaf_rn(-th, ql, rem);
+    const float tl = __fdividef(rem, qh);
+    // q = (d - x) - t as a three-term sum with one renormalisation
+    float s1, e1, s2, e2;
+    two_sum(dh[k], -x.hi, s1, e1);
+    two_sum(s1, -th, s2, e2);
+    const float lo = __fadd_rn(__fadd_rn(e1, e2), __fsub_rn(__fsub_rn(dl[k], x.lo), tl));
+    fast_two_sum(s2, lo, qh, ql);
+    if (fabsf(qh) <= pivmin) {
+      qh = -pivmin;
+      ql = 0.0f;
+    }
+    c += qh < 0.0f;
+  }
+  return c;
+}
+
+// One thread per wanted eigenvalue.  mode 0: FP64 counts from global memory;
+// mode 1: the tridiagonal in shared memory, the interval first narrowed with
+// FP32 Sturm counts (cheap on the FP32 pipes), then widened by a margin far
+// above the FP32 backward error of the count (64 eps32 (||T|| + |x|)),
+// checked with two counts (falling back to the Gerschgorin interval if the
+// check fails) and finished in FP64; mode 2 (mixed form): as mode 1 but
+// checked and finished with double-float counts, whose accuracy floor
+// (a few 2^-44 ||T||) ends the bisection.
 __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *ee, int64_t sd, const int *nvec,
                                                 const int64_t *rng, const double *tinfo, double abstol, double *wout,
-                                                int64_t *info, int use_smem) {
+                                                int64_t *info, int mode) {
   extern __shared__ double sm[];
   const int b = blockIdx.y;
   const int n = nvec[b];
@@ -618,7 +666,9 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
   double *se2 = sm + n;
   float *fd = (float *)(sm + 2 * n);
   float *fe2 = fd + n;
-  if (use_smem) {
+  // mode 2 layout: d.hi, d.lo, e2.hi, e2.lo
+  float *gdh = (float *)sm, *gdl = gdh + n, *ge2h = gdl + n, *ge2l = ge2h + n;
+  if (mode == 1) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
       const double e2 = (k < n - 1) ? e[k] * e[k] : 0.0;
       sd_[k] = d[k];
@@ -627,6 +677,18 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
       fe2[k] = (float)e2;
     }
     __syncthreads();
+  } else if (mode == 2) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const double e2 = (k < n - 1) ? e[k] * e[k] : 0.0;
+      const df dk = df_from(d[k]), ek = df_from(e2);
+      gdh[k] = dk.hi;
+      gdl[k] = dk.lo;
+      ge2h[k] = ek.hi;
+      ge2l[k] = ek.lo;
+    }
+    __syncthreads();
+    fd = gdh;
+    fe2 = ge2h;
   }
   const int64_t lo_idx = rng[b * 8 + 0];
   const int64_t m = rng[b * 8 + 2];
@@ -637,8 +699,10 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
   const double pivmin = tinfo[b * 8 + 3];
   double lo = gl, hi = gu;
   const double ulp = DBL_EPSILON;
+  const float pivdf = fmaxf(1e-30f, (float)pivmin);
   auto count64 = [&](double x) -> int {
-    if (use_smem) return sturm_count(sd_, se2, n, x, pivmin);
+    if (mode == 2) return sturm_count_df(gdh, gdl, ge2h, ge2l, n, df_from(x), pivdf);
+    if (mode == 1) return sturm_count(sd_, se2, n, x, pivmin);
     double q = d[0] - x;
     if (fabs(q) <= pivmin) q = -pivmin;
     int c = q < 0.0;
@@ -649,7 +713,7 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
     }
     return c;
   };
-  if (use_smem && tnorm > 0.0 && tnorm < 1e30) {
+  if (mode != 0 && tnorm > 0.0 && tnorm < 1e30) {
     float lo32 = (float)lo, hi32 = (float)hi;
     const float piv32 = fmaxf(1e-30f, (float)pivmin);
     const float stop = 16.0f * FLT_EPSILON * (float)tnorm;
@@ -667,9 +731,11 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
       hi = h2;
     }
   }
+  // accuracy floor of the double-float count (mode 2)
+  const double floor_df = (mode == 2) ? 4.0 * 0x1p-44 * tnorm : 0.0;
   bool conv = false;
   for (int it = 0; it < 256; ++it) {
-    double tol = fmax(fmax(abstol, pivmin), 2.0 * ulp * fmax(fabs(lo), fabs(hi)));
+    double tol = fmax(fmax(fmax(abstol, pivmin), 2.0 * ulp * fmax(fabs(lo), fabs(hi))), floor_df);
     if (hi - lo <= tol) {
       conv = true;
       break;
@@ -686,9 +752,14 @@ __global__ void __launch_bounds__(128) k_bisect(const double *dd, const double *
 
 // Opt the bisection kernel into the dynamic shared memory it needs for order
 // n (done once per size outside any stream capture).
-cudaError_t prepare_bisect(int n) {
+size_t bisect_smem(int64_t n, int mixed) {
+  const size_t b = mixed ? 4 * (size_t)n * sizeof(float) : 2 * (size_t)n * (sizeof(double) + sizeof(float));
+  return b <= 200 * 1024 ? b : 0;
+}
+
+cudaError_t prepare_bisect(size_t bytes) {
   static std::atomic<int> done{0};
-  const int need = (int)(2 * (size_t)n * (sizeof(double) + sizeof(float)));
+  const int need = (int)bytes;
   if (need <= done.load() || need > 200 * 1024) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
   if (e == cudaSuccess) {
@@ -700,18 +771,17 @@ cudaError_t prepare_bisect(int n) {
 }
 
 cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, int64_t il, int64_t iu, double abstol,
-                                cudaStream_t s) {
+                                cudaStream_t s, int mixed) {
   const int64_t sd = w.nmax;
   k_tdprep<<<w.B, 32, 0, s>>>(w.d, w.e, sd, w.nvec, range, vl, vu, il, iu, w.rng, w.tinfo, w.info);
-  size_t smem = 2 * (size_t)w.nmax * (sizeof(double) + sizeof(float));
-  int use_smem = smem <= 200 * 1024;
-  if (use_smem) {
-    PP_CUDA_TRY(prepare_bisect(w.nmax));
-  } else {
-    smem = 0;
+  const size_t smem = bisect_smem(w.nmax, mixed);
+  int mode = 0;
+  if (smem) {
+    mode = mixed ? 2 : 1;
+    PP_CUDA_TRY(prepare_bisect(smem));
   }
   dim3 g(cdiv(w.nmax, 128), w.B);
-  PP_KT(KT_BISECT, s, (k_bisect<<<g, 128, smem, s>>>(w.d, w.e, sd, w.nvec, w.rng, w.tinfo, abstol, w.w, w.info, use_smem)));
+  PP_KT(KT_BISECT, s, (k_bisect<<<g, 128, smem, s>>>(w.d, w.e, sd, w.nvec, w.rng, w.tinfo, abstol, w.w, w.info, mode)));
   count_launch(2);
   return cudaGetLastError();
 }
@@ -929,6 +999,7 @@ cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
 constexpr int BT_J = 64;     // columns per block
 constexpr int BT_RK = 16;    // rows per k-step
 constexpr int BT_RCH = 512;  // rows per split-K chunk
+constexpr int GRAM_RCH = 64; // rows per chunk of the Gram product V^H V
 
 // Wp[ks][a][j] = sum_{r in chunk ks} conj(V(r,a)) X(r,j) for a < jb.
 // V(r,a) = A(r, k0+a) for r >= k0+a+1 (zero above).  X is E (ncol = m of
@@ -936,7 +1007,7 @@ constexpr int BT_RCH = 512;  // rows per split-K chunk
 template <class R>
 __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Xb, int64_t ldx,
                                              int64_t sX, int x_is_v, const int *nvec, const int64_t *rng, int k0,
-                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp, int ncol_fixed) {
+                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp, int ncol_fixed, int rch) {
   __shared__ C<R> sV[BT_RK][32];
   __shared__ C<R> sXt[BT_RK][BT_J];
   const int b = blockIdx.z;
@@ -944,7 +1015,7 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
   const int ncol = x_is_v ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
   const int j0 = blockIdx.x * BT_J;
   const int ks = blockIdx.y;
-  const int rbeg = k0 + 1 + ks * BT_RCH;
+  const int rbeg = k0 + 1 + ks * rch;
   if (j0 >= ncol || rbeg >= n) return;
   const C<R> *A = Ab + b * sA;
   const C<R> *X = x_is_v ? (A + lda * k0) : (Xb + b * sX);
@@ -953,7 +1024,7 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
   C<R> acc[8];
 #pragma unroll
   for (int p = 0; p < 8; ++p) acc[p] = cz<R>();
-  const int rend = min(n, rbeg + BT_RCH);
+  const int rend = min(n, rbeg + rch);
   for (int r0 = rbeg; r0 < rend; r0 += BT_RK) {
     for (int e = threadIdx.x; e < BT_RK * 32; e += 256) {
       const int a = e & 31, rr = e >> 5;
@@ -1022,6 +1093,19 @@ __global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int6
     }
     Wb[b * sWb + (int64_t)a * ldwp + j] = cfin(acc);
   }
+}
+
+// G = V^H V from the Gram partials of k_vhx (row chunks of GRAM_RCH, stored
+// 32 x 32 per chunk): one thread per entry.
+template <class R>
+__global__ void __launch_bounds__(1024) k_gram_sum(const C<R> *Wp, int64_t sWp, const int *nvec, int k0, z64 *G) {
+  const int b = blockIdx.x;
+  const int n = nvec[b];
+  const int a = threadIdx.x >> 5, j = threadIdx.x & 31;
+  const int nks = (n - k0 - 1 + GRAM_RCH - 1) / GRAM_RCH;
+  C<R> s = cz<R>();
+  for (int ks = 0; ks < nks; ++ks) s = cadd(s, Wp[b * sWp + ((int64_t)ks * 32 + a) * 32 + j]);
+  G[b * 1024 + a * 32 + j] = cto64(s);
 }
 
 // Tf (zlarft, forward, columnwise): Tf(a,a) = tau_a,
@@ -1133,13 +1217,14 @@ cudaError_t back_transform(EigWork &w, cudaStream_t s) {
   for (int k0 = kstart; k0 >= 0; k0 -= nb) {
     const int jb = min(nb, nref - k0);
     const int ks = cdiv(nmax - k0 - 1, BT_RCH);
+    const int ksg = cdiv(nmax - k0 - 1, GRAM_RCH);
     // Tf from G = V^H V
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, ldwp, sWp, 0)));
-    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb, sWb, 0)));
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, 32, sWp, 0, GRAM_RCH)));
+    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
     // Y = Tf V^H E ; E -= V Y
     PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
-                                                             jb, Wp, ldwp, sWp, 0)));
+                                                             jb, Wp, ldwp, sWp, 0, BT_RCH)));
     PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, 0)));
     PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
         A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb, 0)));
@@ -1237,13 +1322,14 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
   for (int k0 = 0; k0 < nref; k0 += nb) {
     const int jb = min(nb, nref - k0);
     const int ks = cdiv(nmax - k0 - 1, BT_RCH);
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ks, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb,
-                                                            Wp, ldwp, sWp, 0)));
-    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(1, B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 0, w.G, w.Tf, Wb,
-                                                            sWb, 0)));
+    const int ksg = cdiv(nmax - k0 - 1, GRAM_RCH);
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb,
+                                                             Wp, 32, sWp, 0, GRAM_RCH)));
+    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
     PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(nrows, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, X, ldx, sX, 0, w.nvec,
-                                                                             w.rng, k0, jb, Wp, ldwp, sWp, nrows)));
+                                                                             w.rng, k0, jb, Wp, ldwp, sWp, nrows,
+                                                                             BT_RCH)));
     PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(nrows, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 2,
                                                                           w.G, w.Tf, Wb, sWb, nrows)));
     PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(

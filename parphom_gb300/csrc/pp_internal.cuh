@@ -128,9 +128,11 @@ cudaError_t backward_phi(const Geometry &g, const double *d_q, const z64 *Z, int
 // Eigen stages, templated on the real type (double / df) in pp_eigen.cu.
 template <class R>
 cudaError_t tridiagonalize(EigWork &w, cudaStream_t s);
-cudaError_t prepare_bisect(int n);
+cudaError_t prepare_bisect(size_t bytes);
+// dynamic shared memory of the bisection kernel for order n (0: global-memory mode)
+size_t bisect_smem(int64_t n, int mixed);
 cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, int64_t il, int64_t iu,
-                                double abstol, cudaStream_t s);
+                                double abstol, cudaStream_t s, int mixed = 0);
 template <class R>
 cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s);
 template <class R>
