@@ -51,6 +51,7 @@ typedef struct pp_ctx pp_ctx;
 #define PP_INFO_NOORTH 2      /* a cluster of eigenvectors not orthogonalised  */
 #define PP_INFO_NOMEM 4       /* workspace too small for all eigenvectors      */
 #define PP_INFO_NOTCOMP 8     /* an eigenvalue was not computed                */
+#define PP_INFO_TIMEOUT 16    /* a bounded device wait gave up: results invalid */
 
 /* Precision forms. */
 #define PP_PREC_FP64 0        /* plain IEEE double throughout                  */

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libparphom_gpu.so")
-SOURCES = ["pp_capi.cu", "pp_dynmat.cu", "pp_eigen.cu", "pp_noalloc.cu", "pp_dos.cu"]
+SOURCES = ["pp_capi.cu", "pp_dynmat.cu", "pp_eigen.cu", "pp_noalloc.cu", "pp_dos.cu", "pp_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
 

@@ -242,6 +242,12 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   w.nbr = nbr;
   add(&w.Xr, 16 * (size_t)B * lda * std::max(nbr, 1));
   add(&w.Eb, 16 * (size_t)B * std::max(nbr, 1) * mcap);
+  // tensor-core trailing update of the double-float form
+  w.sTcS = (int64_t)her2k_tc_bytes(n);
+  w.sTcE = her2k_tc_exps(n);
+  add((void **)&w.tcS, (size_t)B * w.sTcS);
+  add((void **)&w.tcE, 4 * (size_t)B * w.sTcE);
+  add((void **)&w.tcErr, 4 * (size_t)B);
   add((void **)&c->vpart, 8 * (size_t)B * c->nsplit * 3 * mcap + 16 * (size_t)B * nbnd * 3);
   add((void **)&c->vraw, 8 * (size_t)B * 3 * mcap);
   add((void **)&c->d_q, 8 * (size_t)B * 3);
@@ -257,6 +263,8 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
     return PP_ERR_NOMEM;
   }
   for (auto &p : parts) *p.first = (char *)base + p.second;
+  // opt the tensor-core kernel into its shared memory (outside any capture)
+  TRY_CUDA(prepare_her2k_tc());
   c->ws = base;
   c->ws_bytes = off;
   w.bytes = off;
@@ -276,7 +284,7 @@ size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd, int64_t nbr) 
   const int64_t T = std::min<int64_t>(((int64_t)mcap + 63) / 64 * 64, 2048);
   size_t per = 16 * (size_t)n * n + 16 * (size_t)n * mcap + 8 * (size_t)5 * n * T + (size_t)n * T +
                16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
-               16 * (size_t)((n + 63) / 64) * 32 * 32 +
+               16 * (size_t)((n + 63) / 64) * 32 * 32 + her2k_tc_bytes(n) + 8 * (size_t)(n + 128) +
                8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd + 16 * (size_t)nbr * (n + mcap);
   return per * B;
 }
@@ -332,6 +340,11 @@ EigWork view_of(const EigWork &w, int off, int cnt) {
   v.Wp = sh(w.Wp, 16 * (size_t)w.ksplit * 32 * w.ldwp);
   v.Xr = sh(w.Xr, 16 * (size_t)w.lda * std::max(w.nbr, 1));
   v.Eb = sh(w.Eb, 16 * (size_t)std::max(w.nbr, 1) * w.mcap);
+  if (w.tcS) {
+    v.tcS = (uint8_t *)sh(w.tcS, (size_t)w.sTcS);
+    v.tcE = (int *)sh(w.tcE, 4 * (size_t)w.sTcE);
+    v.tcErr = (int *)sh(w.tcErr, 4);
+  }
   return v;
 }
 

@@ -24,6 +24,7 @@
 // form) or df (double-float on the FP32 pipes, the mixed form).
 #include <atomic>
 #include <cfloat>
+#include <type_traits>
 #include <cstdio>
 
 #include "pp_internal.cuh"
@@ -468,6 +469,7 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
   const int B = w.B, nmax = w.nmax, nb = w.nb;
   const int64_t lda = w.lda, sA = w.sA, sW = (int64_t)w.lda * nb, sP = (int64_t)w.nchunk * w.lda;
   const int64_t sd = w.nmax;
+  if (w.tcErr) PP_CUDA_TRY(cudaMemsetAsync(w.tcErr, 0, sizeof(int) * B, s));
   for (int k0 = 0; k0 < nmax; k0 += nb) {
     const int jb = min(nb, nmax - k0);
     int nprev = 0;  // k_wcorr blocks of the previous column, when its w is still to be completed
@@ -504,10 +506,14 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
     }
     const int k1 = k0 + jb;
     if (k1 < nmax) {
-      const int m = nmax - k1;
-      dim3 g(cdiv(m, HK_T), cdiv(m, HK_T), B);
-      PP_KT(KT_HER2K, s, (k_her2k<R><<<g, 256, 0, s>>>(A, lda, sA, W, sW, w.nvec, k0, jb)));
-      count_launch(1);
+      if (std::is_same<R, df>::value && w.tcS && tc_enabled()) {
+        PP_CUDA_TRY(her2k_tc(w, k0, jb, s));
+      } else {
+        const int m = nmax - k1;
+        dim3 g(cdiv(m, HK_T), cdiv(m, HK_T), B);
+        PP_KT(KT_HER2K, s, (k_her2k<R><<<g, 256, 0, s>>>(A, lda, sA, W, sW, w.nvec, k0, jb)));
+        count_launch(1);
+      }
     }
   }
   return cudaGetLastError();
@@ -530,7 +536,8 @@ __device__ __forceinline__ int sturm_count(const double *d, const double *e2, in
 
 // Gerschgorin interval, pivmin and the index range of the wanted eigenvalues.
 __global__ void k_tdprep(const double *dd, const double *ee, int64_t sd, const int *nvec, char range, double vl,
-                         double vu, int64_t il, int64_t iu, int64_t *rng, double *tinfo, int64_t *info) {
+                         double vu, int64_t il, int64_t iu, int64_t *rng, double *tinfo, int64_t *info,
+                         const int *tcerr) {
   const int b = blockIdx.x;
   if (threadIdx.x != 0) return;
   const int n = nvec[b];
@@ -586,7 +593,7 @@ __global__ void k_tdprep(const double *dd, const double *ee, int64_t sd, const i
   tinfo[b * 8 + 1] = gu;
   tinfo[b * 8 + 2] = tnorm;
   tinfo[b * 8 + 3] = pivmin;
-  info[b] = 0;
+  info[b] = (tcerr && tcerr[b]) ? PP_INFO_TIMEOUT : 0;
 }
 
 __device__ __forceinline__ int sturm_count32(const float *d, const float *e2, int n, float x, float pivmin) {
@@ -773,7 +780,7 @@ cudaError_t prepare_bisect(size_t bytes) {
 cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, int64_t il, int64_t iu, double abstol,
                                 cudaStream_t s, int mixed) {
   const int64_t sd = w.nmax;
-  k_tdprep<<<w.B, 32, 0, s>>>(w.d, w.e, sd, w.nvec, range, vl, vu, il, iu, w.rng, w.tinfo, w.info);
+  k_tdprep<<<w.B, 32, 0, s>>>(w.d, w.e, sd, w.nvec, range, vl, vu, il, iu, w.rng, w.tinfo, w.info, w.tcErr);
   const size_t smem = bisect_smem(w.nmax, mixed);
   int mode = 0;
   if (smem) {

@@ -80,6 +80,14 @@ struct EigWork {
   void *Eb = nullptr;     // [B][nbr*mcap]  rows of E = Q Z
   int nbr = 0;
 
+  // tensor-core trailing update (double-float form): bf16 slices of the
+  // panel rows, their exponents, and a per-matrix time-out flag
+  uint8_t *tcS = nullptr; // [B][her2k_tc_bytes(nmax)]
+  int64_t sTcS = 0;
+  int *tcE = nullptr;     // [B][her2k_tc_exps(nmax)] (V, W) exponent pairs per row
+  int64_t sTcE = 0;
+  int *tcErr = nullptr;   // [B]
+
   size_t bytes = 0;
 };
 
@@ -128,6 +136,12 @@ cudaError_t backward_phi(const Geometry &g, const double *d_q, const z64 *Z, int
 // Eigen stages, templated on the real type (double / df) in pp_eigen.cu.
 template <class R>
 cudaError_t tridiagonalize(EigWork &w, cudaStream_t s);
+// Trailing update of panel k0 on the tensor cores (double-float storage).
+cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s);
+size_t her2k_tc_bytes(int64_t nmax);
+int64_t her2k_tc_exps(int64_t nmax);
+cudaError_t prepare_her2k_tc();
+bool tc_enabled();
 cudaError_t prepare_bisect(size_t bytes);
 // dynamic shared memory of the bisection kernel for order n (0: global-memory mode)
 size_t bisect_smem(int64_t n, int mixed);

@@ -3,10 +3,13 @@
 Frequencies: |dw| < 1e-4 cm^-1 absolute or 1e-8 relative for |w| >= W_MIN;
 below W_MIN (acoustic modes at/near Gamma, where the square root amplifies
 FP64 rounding) the eigenvalues of D are compared: |dlambda| <= 64 n eps ||D||.
-Velocities: per mode |dv| <= 1e-6 max(|v|, 1e-3 max_q|v|) on modes whose
+Velocities: per mode |dv| <= 1e-6 max(|v|, 1e-3 max|v|) on modes whose
 eigenvalue is separated from its neighbours by more than 1e-6 ||D||; inside
 clusters closer than that (degenerate or nearly so) the per-mode velocity is
 basis dependent and the cluster sums are compared with the same rule.
+max|v| is taken over every mode and q-point of the compared set: at Gamma
+all velocities are rounding noise divided by the reference's 1e-3 clamp, so
+a per-q scale would ask for agreement of that noise.
 Eigenvectors: residual ||D z - lambda z|| <= RES_TOL ||D|| and
 ||Z^H Z - I||_max <= ORTH_TOL, plus per-cluster projector distance.
 """
