@@ -21,7 +21,7 @@
 // both at full relative resolution; the dropped pairs and the residual bound
 // the error by about 2^-55 |X_r| |Y_c| per product, the double-float level.
 //
-// CTA (256 threads) = 128 rows x (up to 8) column blocks of 32, both
+// CTA (512 threads) = 128 rows x (up to 8) column blocks of 32, both
 // products in turn.  The 112 KB row operand stays in shared memory while the
 // 28 KB column operands are streamed in by bulk copies, double-buffered so
 // that the next block's copy overlaps this block's MMAs.  One CTA per SM
@@ -45,6 +45,8 @@ constexpr int TC_OP = TC_S * TC_KS * TC_TILE;    // one operand of a 128-row blo
 constexpr int TC_RBLK = 2 * TC_OP;               // V and W operands of a 128-row block
 constexpr int TC_BBYTES = TC_S * TC_KS * 1024;   // one 32-row column block of one operand (28672)
 constexpr int TC_CB = 8;                         // column blocks per CTA
+constexpr int TC_NT = 512;                       // threads: 16 warps = 4 lane groups x 4 column quarters
+constexpr int TC_CQ = 32 / (TC_NT / 128);        // columns per thread in the epilogue (8)
 constexpr int TC_SMEM = TC_OP + 2 * TC_BBYTES + 2 * 256 + 64;  // + 2 x 32 exponent pairs, mbarriers, TMEM slot
 constexpr int TC_NACC = 2 * TC_S;                // accumulators: (re, im) x slice-sum group
 constexpr uint32_t TC_ID = tc::idesc_bf16(128, 32, 0);
@@ -138,19 +140,22 @@ __device__ __forceinline__ df combine7(const float *acc) {
 }
 
 // MMAs of one column block: re acc pairs row k-step j with column k-step j,
-// im acc with column k-step j ^ 2, negated for j < 2 (Re X . Im Y).
+// im acc with column k-step j ^ 2, negated for j < 2 (Re X . Im Y).  Fully
+// unrolled: a descriptor differs from the block's first only in its start
+// address (bits 0-13, in 16-byte units), so each MMA costs one add.
 __device__ __forceinline__ void tc_issue(uint32_t tm, uint32_t sa, uint32_t sb) {
-#pragma unroll 1
+  const uint64_t a0 = tc::sdesc(sa, 128, 256), b0 = tc::sdesc(sb, 128, 256);
+#pragma unroll
   for (int u = 0; u < TC_S; ++u) {
-#pragma unroll 1
+#pragma unroll
     for (int s = 0; s <= u; ++s) {
       const int t = u - s;
 #pragma unroll
       for (int j = 0; j < TC_KS; ++j) {
         const uint32_t acc = (s == 0 && j == 0) ? 0u : 1u;
-        const uint64_t ad = tc::sdesc(sa + (s * TC_KS + j) * TC_TILE, 128, 256);
-        const uint64_t br = tc::sdesc(sb + (t * TC_KS + j) * 1024, 128, 256);
-        const uint64_t bi = tc::sdesc(sb + (t * TC_KS + (j ^ 2)) * 1024, 128, 256);
+        const uint64_t ad = a0 + (uint64_t)((s * TC_KS + j) * (TC_TILE >> 4));
+        const uint64_t br = b0 + (uint64_t)((t * TC_KS + j) * (1024 >> 4));
+        const uint64_t bi = b0 + (uint64_t)((t * TC_KS + (j ^ 2)) * (1024 >> 4));
         tc::mma_bf16(tm + u * 32, ad, br, TC_ID, acc);
         tc::mma_bf16(tm + (TC_S + u) * 32, ad, bi, j < 2 ? TC_IDN : TC_ID, acc);
       }
@@ -158,7 +163,7 @@ __device__ __forceinline__ void tc_issue(uint32_t tm, uint32_t sa, uint32_t sb) 
   }
 }
 
-__global__ void __launch_bounds__(256, 1) k_her2k_tc(zdf *Ab, int64_t lda, int64_t sA, const uint8_t *S, int64_t sS,
+__global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int64_t sA, const uint8_t *S, int64_t sS,
                                                      const int *Ex, int64_t sEx, const int *nvec, int k0, int jb,
                                                      int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -215,11 +220,11 @@ __global__ void __launch_bounds__(256, 1) k_her2k_tc(zdf *Ab, int64_t lda, int64
     // copied whole; the product picks its half
     tc::bulk_g2s(sEc + buf * 64, Eb + 2 * 32 * cb, 256, bar);
   };
-  const int lg = warp & 3, chalf = warp >> 2;
+  const int lg = warp & 3, cqt = warp >> 2;
   const int rl = 128 * R + 32 * lg + (tid & 31);  // trailing-block row = TMEM lane
   const int r = k1 + rl;
   const int Erv = Eb[2 * rl], Erw = Eb[2 * rl + 1];
-  const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + 16 * chalf;
+  const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + TC_CQ * cqt;
   const uint32_t sa = tc::smem_u32(sAop);
   int ok = 1;
   for (int i = 0; i < nblk; ++i) {
@@ -250,10 +255,10 @@ __global__ void __launch_bounds__(256, 1) k_her2k_tc(zdf *Ab, int64_t lda, int64
       if (!good) atomicExch(&err[b], 1);
     }
     // this thread's 16 entries of A, loaded while the MMAs run
-    zdf cv[16];
-    const int cbase = k1 + 32 * cb + 16 * chalf;
+    zdf cv[TC_CQ];
+    const int cbase = k1 + 32 * cb + TC_CQ * cqt;
 #pragma unroll
-    for (int qq = 0; qq < 16; ++qq) {
+    for (int qq = 0; qq < TC_CQ; ++qq) {
       const int c = cbase + qq;
       if (r < n && c < n && r >= c) cv[qq] = A[r + lda * c];
     }
@@ -266,7 +271,7 @@ __global__ void __launch_bounds__(256, 1) k_her2k_tc(zdf *Ab, int64_t lda, int64
     const int erow = p == 0 ? Erv : Erw;
     const int *ec = sEc + (i & 1) * 64;  // (V, W) exponent pairs of the column rows
 #pragma unroll
-    for (int cc = 0; cc < 4; ++cc) {
+    for (int cc = 0; cc < TC_CQ / 4; ++cc) {
       float are[TC_S][4], aim[TC_S][4];
 #pragma unroll
       for (int u = 0; u < TC_S; ++u) {
@@ -286,7 +291,7 @@ __global__ void __launch_bounds__(256, 1) k_her2k_tc(zdf *Ab, int64_t lda, int64
             vi[u] = aim[u][qq];
           }
           // column exponent: W half for the first product, V half for the second
-          const int ecol = ec[2 * (16 * chalf + q16) + (p == 0 ? 1 : 0)];
+          const int ecol = ec[2 * (TC_CQ * cqt + q16) + (p == 0 ? 1 : 0)];
           const float sc = pow2f(erow + ecol - 16);
           df pr = combine7(vr), pi = combine7(vi);
           pr.hi = __fmul_rn(pr.hi, sc);
@@ -351,7 +356,7 @@ cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s) {
                                                                       (int64_t)w.lda * w.nb, w.nvec, k0, jb, w.tcS,
                                                                       w.sTcS, w.tcE, w.sTcE)));
   const int nq = (4 * nrb + TC_CB - 1) / TC_CB;
-  PP_KT(KT_HER2K, s, (k_her2k_tc<<<dim3(nq, nrb, w.B), 256, TC_SMEM, s>>>((zdf *)w.A, w.lda, w.sA, w.tcS, w.sTcS,
+  PP_KT(KT_HER2K, s, (k_her2k_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>((zdf *)w.A, w.lda, w.sA, w.tcS, w.sTcS,
                                                                           w.tcE, w.sTcE, w.nvec, k0, jb, w.tcErr)));
   count_launch(2);
   return cudaGetLastError();
