@@ -7,9 +7,12 @@ Velocities: per mode |dv| <= 1e-6 max(|v|, 1e-3 max|v|) on modes whose
 eigenvalue is separated from its neighbours by more than 1e-6 ||D||; inside
 clusters closer than that (degenerate or nearly so) the per-mode velocity is
 basis dependent and the cluster sums are compared with the same rule.
-max|v| is taken over every mode and q-point of the compared set: at Gamma
-all velocities are rounding noise divided by the reference's 1e-3 clamp, so
-a per-q scale would ask for agreement of that noise.
+max|v| is taken over every mode and q-point of the compared set.  Modes at
+the reference's clamp (2|w| < 1e-3 cm^-1: the acoustic modes at Gamma) have
+a numerator at the eigensolver's backward-error level divided by the clamp
+constant, i.e. rounding noise: a normwise perturbation of 1e-15 ||D|| moves
+their cluster sum by ~1e-6 m/s, 1e-14 by ~3e-5 m/s.  They are compared with
+|dv| <= 1e-7 max|v| (a few mm/s on a 2e4 m/s band).
 Eigenvectors: residual ||D z - lambda z|| <= RES_TOL ||D|| and
 ||Z^H Z - I||_max <= ORTH_TOL, plus per-cluster projector distance.
 """
@@ -22,6 +25,8 @@ W_ABS = 1e-4
 W_REL = 1e-8
 V_REL = 1e-6
 GAP_REL = 1e-6
+CLAMP = 1e-3      # write_output.F90:443: v = Re(e^H dD e) / max(2|w|, 1e-3)
+V_CLAMP = 1e-7
 
 
 def clusters(lam, norm):
@@ -53,10 +58,15 @@ def check_frequencies(w_gpu, w_ref, lam_ref, n, Dnorm):
 
 def check_velocities(v_gpu, v_ref, lam_ref, Dnorm, vmax):
     floor = max(1e-3 * vmax, 1e-6)
+    w_ref = np.sign(lam_ref) * np.sqrt(np.abs(lam_ref)) * O.C1 * O.C2
     worst = 0.0
     for g in clusters(lam_ref, Dnorm):
         a = v_gpu[g].sum(axis=0)
         b = v_ref[g].sum(axis=0)
+        if np.all(2.0 * np.abs(w_ref[g]) < CLAMP):
+            # the reference divides by its clamp constant: rounding noise only
+            assert np.all(np.abs(a - b) <= V_CLAMP * vmax), (g, a, b)
+            continue
         tol = V_REL * np.maximum(np.abs(b), floor)
         rel = np.abs(a - b) / np.maximum(np.abs(b), floor)
         worst = max(worst, float(rel.max()))
