@@ -154,7 +154,7 @@ class Result:
     m: np.ndarray          # (nq,) eigenvalues found
     nz: np.ndarray         # (nq,) eigenvectors computed
     w: np.ndarray          # (nq, n) frequencies (cm^-1) or eigenvalues; entries >= m are unset
-    z: Optional[np.ndarray]    # (nq, n, n) complex, column j = eigenvector j (Fortran layout per q)
+    z: Optional[np.ndarray]    # (nq, n, mz) complex, column j = eigenvector j; mz = n, or iu-il+1 for range I
     vel: Optional[np.ndarray]  # (nq, n, 3) m/s
     info: np.ndarray       # (nq,) pzheevx-style bits
 
@@ -229,11 +229,13 @@ class PhononContext:
         info = np.zeros(nq, np.int64)
         w = np.zeros((nq, n))
         vecs = opts.jobz == "V" or opts.vel
-        z = np.zeros((nq, n, n), np.complex128) if (vecs and want_z) else None
+        # eigenvector columns per q: all of them, or the index range
+        mz = int(opts.iu - opts.il + 1) if opts.range == "I" else n
+        z = np.zeros((nq, mz, n), np.complex128) if (vecs and want_z) else None
         vel = np.zeros((nq, n, 3)) if opts.vel else None
         zv = z.view(np.float64) if z is not None else None
         rv = PPResultView(m.ctypes.data_as(_ip), nz.ctypes.data_as(_ip), _p(w), n,
-                          _p(zv) if zv is not None else None, n, 2 * n * n,
+                          _p(zv) if zv is not None else None, n, 2 * n * mz,
                           _p(vel) if vel is not None else None, 3 * n, None)
         oc = opts.to_c()
         rc = self._lib.pp_solve_batch(self._h, qf.ctypes.data_as(_dp), nq, nq, ctypes.byref(oc), ctypes.byref(rv),
@@ -242,7 +244,7 @@ class PhononContext:
             raise PPError(rc, "pp_solve_batch")
         if z is not None:
             # per q the buffer holds z[2*(r + n*j)] (column-major) -> numpy (r, j)
-            z = np.ascontiguousarray(z.reshape(nq, n, n).transpose(0, 2, 1))
+            z = np.ascontiguousarray(z.transpose(0, 2, 1))
         return Result(m=m, nz=nz, w=w, z=z, vel=vel, info=info)
 
 
