@@ -1,8 +1,8 @@
-"""Build libparphom_gpu.so (the C-ABI library) in-tree with nvcc for sm_103a.
+"""Build libparphom_gpu.so (the C-ABI library) in-tree with nvcc for sm_103a,
+and the native host driver parphom_gpu.x (C++, linked against it).
 
 Translation units are compiled in parallel and linked with the CUDA runtime;
-the result lands in parphom_gb300/lib/.  No PyTorch is involved in the
-library itself.
+the results land in parphom_gb300/lib/.  No PyTorch is involved in either.
 """
 from __future__ import annotations
 
@@ -17,6 +17,9 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libparphom_gpu.so")
+HOST = os.path.join(HERE, "host")
+EXE = os.path.join(LIBDIR, "parphom_gpu.x")
+HOST_SOURCES = ["h5min.cpp", "inputs.cpp", "parphom_gpu_main.cpp"]
 SOURCES = ["pp_capi.cu", "pp_dynmat.cu", "pp_eigen.cu", "pp_noalloc.cu", "pp_dos.cu", "pp_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
@@ -62,5 +65,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+def build_host(force: bool = False) -> str:
+    """The host driver: g++, no contraction of a*b+c (the geometry matches
+    the reference's evaluation order), rpath to the library's directory."""
+    lib = build()
+    srcs = [os.path.join(HOST, f) for f in HOST_SOURCES]
+    deps = [lib, os.path.join(HERE, "..", "include", "parphom_gpu.h")] + srcs + \
+        [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".hpp")]
+    if not force and os.path.exists(EXE) and os.path.getmtime(EXE) >= max(os.path.getmtime(f) for f in deps):
+        return EXE
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = EXE + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(HERE, "..", "include"), *srcs,
+           "-o", tmp, "-L", LIBDIR, "-lparphom_gpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host driver build failed:\n{r.stderr}")
+    os.replace(tmp, EXE)
+    return EXE
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_host(force="--force" in sys.argv))
