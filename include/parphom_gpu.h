@@ -55,8 +55,10 @@ typedef struct pp_ctx pp_ctx;
 
 /* Precision forms. */
 #define PP_PREC_FP64 0        /* plain IEEE double throughout                  */
-#define PP_PREC_MIXED 1       /* O(n^3) stages in double-float on FP32 pipes,
-                                 FP64 in the tridiagonal solve and velocities  */
+#define PP_PREC_MIXED 1       /* reduction and back-transform in double-float
+                                 on the FP32 pipes, the trailing update on the
+                                 tensor cores (exact bf16 slice products),
+                                 FP64 inverse iteration and velocities       */
 
 /* pp_ctx_create flags. */
 #define PP_FLAG_ENFORCE_ASR 1 /* reset Phi_II = -sum_{J!=I} Phi_IJ (off by
