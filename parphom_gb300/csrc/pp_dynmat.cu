@@ -483,14 +483,15 @@ template <int EFMT>
 __global__ void k_finalize(const double *ww, int64_t sd, const int64_t *rng, const int64_t *info_in, int raw,
                            const double *vraw, int64_t mstride, int want_vel, double *wout, int64_t ldw,
                            double *vout, int64_t velstride, int64_t *m_out, int64_t *nz_out, int64_t *info_out,
-                           int jobz_v) {
+                           int jobz_v, const int *tcerr) {
   const int b = blockIdx.y;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t m = rng[b * 8 + 2];
   if (j == 0) {
     if (m_out) m_out[b] = m;
     if (nz_out) nz_out[b] = jobz_v ? m : 0;
-    if (info_out) info_out[b] = info_in[b];
+    // a time-out of a tensor-core launch after the eigenvalues (back-transform)
+    if (info_out) info_out[b] = info_in[b] | ((tcerr && tcerr[b]) ? PP_INFO_TIMEOUT : 0);
   }
   if (j >= m) return;
   const double lam = ww[b * sd + j];
@@ -529,10 +530,10 @@ cudaError_t finalize_outputs(EigWork &w, int efmt, int raw_lambda, const double 
   dim3 g(cdiv(w.nmax, 128), w.B);
   if (efmt == 0)
     k_finalize<0><<<g, 128, 0, s>>>(w.w, w.nmax, w.rng, w.info, raw_lambda, d_vraw, mstride, want_vel, w_out, ldw,
-                                    vel_out, velstride, m_out, nz_out, info_out, jobz_v);
+                                    vel_out, velstride, m_out, nz_out, info_out, jobz_v, w.tcErr);
   else
     k_finalize<1><<<g, 128, 0, s>>>(w.w, w.nmax, w.rng, w.info, raw_lambda, d_vraw, mstride, want_vel, w_out, ldw,
-                                    vel_out, velstride, m_out, nz_out, info_out, jobz_v);
+                                    vel_out, velstride, m_out, nz_out, info_out, jobz_v, w.tcErr);
   count_launch(1);
   if (want_z && z_out) {
     dim3 gz(cdiv(w.nmax, 128), w.mcap, w.B);

@@ -1339,8 +1339,12 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
                                                                              BT_RCH)));
     PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(nrows, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 2,
                                                                           w.G, w.Tf, Wb, sWb, nrows)));
-    PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(
-                            A, w.lda, w.sA, Wb, ldwp, sWb, X, ldx, sX, w.nvec, w.rng, k0, jb, nrows)));
+    if (std::is_same<R, df>::value && w.tcS && tc_enabled()) {
+      PP_CUDA_TRY(applyV_tc(w, k0, jb, (zdf *)X, ldx, sX, (const zdf *)Wb, ldwp, sWb, nrows, s));
+    } else {
+      PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(
+                              A, w.lda, w.sA, Wb, ldwp, sWb, X, ldx, sX, w.nvec, w.rng, k0, jb, nrows)));
+    }
     count_launch(6);
   }
   // Eb = X^H Z

@@ -138,6 +138,10 @@ template <class R>
 cudaError_t tridiagonalize(EigWork &w, cudaStream_t s);
 // Trailing update of panel k0 on the tensor cores (double-float storage).
 cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s);
+// X(k0+1:n, 0:ncols) -= V Y (compact-WY back-transform update) on the tensor
+// cores: V the Householder vectors of panel k0, Y (jb x ncols) at Yb[a ldy + c].
+cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t sX, const zdf *Yb, int64_t ldy,
+                      int64_t sY, int ncols, cudaStream_t s);
 size_t her2k_tc_bytes(int64_t nmax);
 int64_t her2k_tc_exps(int64_t nmax);
 cudaError_t prepare_her2k_tc();

@@ -84,35 +84,38 @@ __device__ __forceinline__ int slice_row(zdf x, uint8_t *blk, int row, int lane)
   return E;
 }
 
-// Slices of the panel rows k1 + rl, rl < 128 * ceil((n - k1)/128): one warp
-// per row.  Block R of the slice array holds the V operand of rows
-// 128R .. 128R+127 followed by their W operand; Ex[2 rl] and Ex[2 rl + 1]
-// are the two row exponents.
-__global__ void __launch_bounds__(128) k_tc_slices(const zdf *Ab, int64_t lda, int64_t sA, const zdf *Wb,
-                                                   int64_t sW, const int *nvec, int k0, int jb, uint8_t *S,
-                                                   int64_t sS, int *Ex, int64_t sEx) {
+// Source rows of one operand: element (row, a) of matrix b is
+// P[b * sP + (rbase + row) * rs + a * cs] (conjugated when conj), zero for
+// a >= min(jb, n_b - 1 - k0) and, with vmask, for rbase + row < k0 + a + 1
+// (the zero part of a Householder panel).  Rows 0 .. nrows_b - 1 exist, with
+// nrows_b = n_b - rbase (nrows_fixed == 0) or nrows_fixed.
+struct TcSliceSrc {
+  const zdf *P;
+  int64_t sP, rs, cs;
+  int rbase, nrows_fixed, vmask, conj;
+};
+
+// Slices of rows 0 .. 128 ceil(nrows_b / 128) - 1 (rows past nrows_b are
+// zero): one warp per row.  Row r of matrix b goes to block r / 128 of
+// S + b sS (blocks blk bytes apart), its exponent to E[b sE + r es + eo].
+__global__ void __launch_bounds__(128) k_tc_slices(TcSliceSrc src, const int *nvec, int k0, int jb, uint8_t *S,
+                                                   int64_t sS, int64_t blk, int *E, int64_t sE, int es, int eo) {
   const int b = blockIdx.y;
   const int n = nvec[b];
-  const int k1 = k0 + jb;
-  const int m = n - k1;
-  if (m <= 0) return;
+  const int nrows = src.nrows_fixed > 0 ? src.nrows_fixed : n - src.rbase;
+  if (nrows <= 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rl = blockIdx.x * 4 + warp;
-  if (rl >= (m + 127) / 128 * 128) return;
-  const int r = k1 + rl;
+  if (rl >= (nrows + 127) / 128 * 128) return;
   const int jmax = min(jb, n - 1 - k0);
-  zdf v{{0.f, 0.f}, {0.f, 0.f}}, w{{0.f, 0.f}, {0.f, 0.f}};
-  if (r < n && lane < jmax) {
-    v = Ab[b * sA + r + lda * (k0 + lane)];
-    w = Wb[b * sW + r + lda * lane];
+  zdf v{{0.f, 0.f}, {0.f, 0.f}};
+  if (rl < nrows && lane < jmax && (!src.vmask || src.rbase + rl >= k0 + lane + 1)) {
+    v = src.P[b * src.sP + (int64_t)(src.rbase + rl) * src.rs + (int64_t)lane * src.cs];
+    if (src.conj) v.im = df_neg(v.im);
   }
-  uint8_t *blk = S + b * sS + (int64_t)(rl >> 7) * TC_RBLK;
-  const int ev = slice_row(v, blk, rl & 127, lane);
-  const int ew = slice_row(w, blk + TC_OP, rl & 127, lane);
-  if (lane == 0) {
-    Ex[b * sEx + 2 * rl] = ev;
-    Ex[b * sEx + 2 * rl + 1] = ew;
-  }
+  uint8_t *blkp = S + b * sS + (int64_t)(rl >> 7) * blk;
+  const int e = slice_row(v, blkp, rl & 127, lane);
+  if (lane == 0) E[b * sE + (int64_t)rl * es + eo] = e;
 }
 
 __device__ __forceinline__ df df_add_f(df a, float b) {
@@ -163,13 +166,33 @@ __device__ __forceinline__ void tc_issue(uint32_t tm, uint32_t sa, uint32_t sb) 
   }
 }
 
-__global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int64_t sA, const uint8_t *S, int64_t sS,
-                                                     const int *Ex, int64_t sEx, const int *nvec, int k0, int jb,
-                                                     int *err) {
+// One operand of a product C -= X Y^H: slices in 128-row blocks of TC_OP
+// bytes placed blk bytes apart (matrix b at S + b sS), and the exponent of
+// row r at E[b sE + r es + eo].
+struct TcOperand {
+  const uint8_t *S;
+  int64_t sS, blk;
+  const int *E;
+  int64_t sE;
+  int es, eo;
+};
+// C(rbase + r, cbase + c) -= sum_p X_p(r, :) Y_p(c, :)^H over the tiles of
+// 128 rows x 32 columns of rows [0, nrows_b) and columns [0, ncols_b): all of
+// them, or (tri) the lower triangle of a square trailing block.
+struct TcUpdate {
+  zdf *C;
+  int64_t ldc, sC;
+  int rbase, cbase;
+  int ncols_fixed;  // columns: ncols_fixed, or n_b - cbase when 0; rows: n_b - rbase
+  int tri, nprod;
+  TcOperand x[2], y[2];
+};
+
+__global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nvec, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *sAop = smem;                                  // row operand
   uint8_t *sBop = smem + TC_OP;                          // two column-operand buffers
-  int *sEc = (int *)(smem + TC_OP + 2 * TC_BBYTES);      // two x 32 (V, W) column exponent pairs
+  int *sEc = (int *)(smem + TC_OP + 2 * TC_BBYTES);      // two x 64 column exponents
   // mbarriers: [0] row operand landed (waited by thread 0), [1], [2] column
   // buffer 0 / 1 landed, [3] MMAs of the block done.
   // Each barrier a thread waits on completes exactly once between two of
@@ -178,18 +201,19 @@ __global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int
   uint32_t *tslot = (uint32_t *)(bars + 4);
   const int b = blockIdx.z, R = blockIdx.y, q = blockIdx.x;
   const int n = nvec[b];
-  const int k1 = k0 + jb;
-  const int m = n - k1;
-  if (m <= 0) return;
-  const int nrb = (m + 127) / 128, ncb = (m + 31) / 32;
+  const int nrows = n - u.rbase;
+  const int ncols = u.ncols_fixed > 0 ? u.ncols_fixed : n - u.cbase;
+  if (nrows <= 0 || ncols <= 0) return;
+  const int nrb = (nrows + 127) / 128, ncb = (ncols + 31) / 32;
   if (R >= nrb) return;
   const int cb_beg = q * TC_CB;
-  const int cb_end = min(min(cb_beg + TC_CB, 4 * (R + 1)), ncb);
+  int cb_end = min(cb_beg + TC_CB, ncb);
+  if (u.tri) cb_end = min(cb_end, 4 * (R + 1));
   if (cb_beg >= cb_end) return;
   // an earlier wait of this matrix gave up: its results are already invalid
   if (*(volatile int *)&err[b]) return;
   const int ncbw = cb_end - cb_beg;
-  const int nblk = 2 * ncbw;  // (product, column block) steps
+  const int nblk = u.nprod * ncbw;  // (product, column block) steps
 
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) tc::tmem_alloc(tslot, 512);
@@ -201,29 +225,27 @@ __global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int
   __syncthreads();
   tc::fence_after();
   const uint32_t tm = *tslot;
-  const uint8_t *Sb = S + b * sS;
-  const int *Eb = Ex + b * sEx;
-  zdf *A = Ab + b * sA;
-  const int r0 = k1 + 128 * R;
-  const int nr = min(128, n - r0);
-  // column operand of step i: product p = i / ncbw uses the W (p = 0) or V
-  // (p = 1) slices of the column rows
+  zdf *C = u.C + b * u.sC;
+  const int r0 = u.rbase + 128 * R;  // first global row of this row block
+  const int nr = min(128, nrows - 128 * R);
+  // column operand of step i (product i / ncbw, column block cb)
   auto issue_cols = [&](int i) {
-    const int p = i / ncbw, cb = cb_beg + i % ncbw;
+    const TcOperand &y = u.y[i / ncbw];
+    const int cb = cb_beg + i % ncbw;
     const int buf = i & 1;
     uint64_t *bar = &bars[1 + buf];
-    tc::mbar_expect_tx(bar, TC_BBYTES + 256);
-    const uint8_t *src = Sb + (int64_t)(cb >> 2) * TC_RBLK + (p == 0 ? TC_OP : 0) + (cb & 3) * 1024;
+    const uint32_t ebytes = 32u * 4u * (uint32_t)y.es;
+    tc::mbar_expect_tx(bar, TC_BBYTES + ebytes);
+    const uint8_t *src = y.S + b * y.sS + (int64_t)(cb >> 2) * y.blk + (cb & 3) * 1024;
     uint8_t *dst = sBop + buf * TC_BBYTES;
     for (int sj = 0; sj < TC_S * TC_KS; ++sj) tc::bulk_g2s(dst + sj * 1024, src + sj * TC_TILE, 1024, bar);
-    // exponents of the 32 column rows (interleaved V, W pairs: 256 bytes),
-    // copied whole; the product picks its half
-    tc::bulk_g2s(sEc + buf * 64, Eb + 2 * 32 * cb, 256, bar);
+    tc::bulk_g2s(sEc + buf * 64, y.E + b * y.sE + (int64_t)32 * cb * y.es, ebytes, bar);
   };
   const int lg = warp & 3, cqt = warp >> 2;
-  const int rl = 128 * R + 32 * lg + (tid & 31);  // trailing-block row = TMEM lane
-  const int r = k1 + rl;
-  const int Erv = Eb[2 * rl], Erw = Eb[2 * rl + 1];
+  const int rl = 128 * R + 32 * lg + (tid & 31);  // row within the block of rows = TMEM lane
+  const int r = u.rbase + rl;
+  int erow[2] = {0, 0};
+  for (int p = 0; p < u.nprod; ++p) erow[p] = u.x[p].E[b * u.x[p].sE + (int64_t)rl * u.x[p].es + u.x[p].eo];
   const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + TC_CQ * cqt;
   const uint32_t sa = tc::smem_u32(sAop);
   int ok = 1;
@@ -234,16 +256,18 @@ __global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int
     if (tid == 0) {
       if (i % ncbw == 0) {
         // row operand of product p (the previous product's MMAs are done)
+        const TcOperand &x = u.x[p];
         tc::mbar_expect_tx(&bars[0], TC_OP);
-        const uint8_t *src = Sb + (int64_t)R * TC_RBLK + (p == 0 ? 0 : TC_OP);
+        const uint8_t *src = x.S + b * x.sS + (int64_t)R * x.blk;
         for (int s = 0; s < TC_S; ++s)
           tc::bulk_g2s(sAop + s * (TC_KS * TC_TILE), src + s * (TC_KS * TC_TILE), TC_KS * TC_TILE, &bars[0]);
       }
       if (i == 0) issue_cols(0);
       if (i + 1 < nblk) issue_cols(i + 1);
-      if (p == 0 && i + 1 < ncbw) {
-        const int c0 = k1 + 32 * (cb + 1);
-        for (int c = c0; c < min(c0 + 32, n); ++c) tc::prefetch_l2(A + r0 + lda * c, (uint32_t)nr * 16u);
+      if (p == 0 && i + 1 < ncbw) {  // the next tile of C towards L2
+        const int c0 = u.cbase + 32 * (cb + 1);
+        for (int c = c0; c < min(c0 + 32, u.cbase + ncols); ++c)
+          tc::prefetch_l2(C + r0 + u.ldc * c, (uint32_t)nr * 16u);
       }
       if (i % ncbw == 0) good = tc::mbar_wait(&bars[0], (uint32_t)p);
       good = good && tc::mbar_wait(&bars[1 + (i & 1)], (uint32_t)((i >> 1) & 1));
@@ -254,13 +278,13 @@ __global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int
       tc::mma_commit(&bars[3]);
       if (!good) atomicExch(&err[b], 1);
     }
-    // this thread's 16 entries of A, loaded while the MMAs run
+    // this thread's entries of C, loaded while the MMAs run
     zdf cv[TC_CQ];
-    const int cbase = k1 + 32 * cb + TC_CQ * cqt;
+    const int cl0 = 32 * cb + TC_CQ * cqt;  // first column (local) of this thread
 #pragma unroll
     for (int qq = 0; qq < TC_CQ; ++qq) {
-      const int c = cbase + qq;
-      if (r < n && c < n && r >= c) cv[qq] = A[r + lda * c];
+      const int cl = cl0 + qq, c = u.cbase + cl;
+      if (rl < nrows && cl < ncols && (!u.tri || r >= c)) cv[qq] = C[r + u.ldc * c];
     }
     bool done = tc::mbar_wait(&bars[3], par3);
     // (already complete: makes the copied column exponents visible here)
@@ -268,31 +292,31 @@ __global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int
     ok = __syncthreads_and(done && ok && good);
     if (!ok) break;
     tc::fence_after();
-    const int erow = p == 0 ? Erv : Erw;
-    const int *ec = sEc + (i & 1) * 64;  // (V, W) exponent pairs of the column rows
+    const int er = erow[p];
+    const TcOperand &y = u.y[p];
+    const int *ec = sEc + (i & 1) * 64;
 #pragma unroll
     for (int cc = 0; cc < TC_CQ / 4; ++cc) {
       float are[TC_S][4], aim[TC_S][4];
 #pragma unroll
-      for (int u = 0; u < TC_S; ++u) {
-        tc::tmem_ld4(lane_addr + u * 32 + cc * 4, are[u]);
-        tc::tmem_ld4(lane_addr + (TC_S + u) * 32 + cc * 4, aim[u]);
+      for (int uu = 0; uu < TC_S; ++uu) {
+        tc::tmem_ld4(lane_addr + uu * 32 + cc * 4, are[uu]);
+        tc::tmem_ld4(lane_addr + (TC_S + uu) * 32 + cc * 4, aim[uu]);
       }
       tc::tmem_ld_wait();
 #pragma unroll
       for (int qq = 0; qq < 4; ++qq) {
         const int q16 = 4 * cc + qq;
-        const int c = cbase + q16;
-        if (r < n && c < n && r >= c) {
+        const int cl = cl0 + q16, c = u.cbase + cl;
+        if (rl < nrows && cl < ncols && (!u.tri || r >= c)) {
           float vr[TC_S], vi[TC_S];
 #pragma unroll
-          for (int u = 0; u < TC_S; ++u) {
-            vr[u] = are[u][qq];
-            vi[u] = aim[u][qq];
+          for (int uu = 0; uu < TC_S; ++uu) {
+            vr[uu] = are[uu][qq];
+            vi[uu] = aim[uu][qq];
           }
-          // column exponent: W half for the first product, V half for the second
-          const int ecol = ec[2 * (TC_CQ * cqt + q16) + (p == 0 ? 1 : 0)];
-          const float sc = pow2f(erow + ecol - 16);
+          const int ecol = ec[(TC_CQ * cqt + q16) * y.es + y.eo];
+          const float sc = pow2f(er + ecol - 16);
           df pr = combine7(vr), pi = combine7(vi);
           pr.hi = __fmul_rn(pr.hi, sc);
           pr.lo = __fmul_rn(pr.lo, sc);
@@ -301,7 +325,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_her2k_tc(zdf *Ab, int64_t lda, int
           zdf a = cv[q16];
           a.re = df_sub(a.re, pr);
           a.im = df_sub(a.im, pi);
-          A[r + lda * c] = a;
+          C[r + u.ldc * c] = a;
         }
       }
     }
@@ -341,24 +365,88 @@ int64_t her2k_tc_exps(int64_t nmax) { return 2 * ((nmax + 127) / 128) * 128; }
 cudaError_t prepare_her2k_tc() {
   static int done = 0;
   if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_her2k_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_cupd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   if (e == cudaSuccess) done = 1;
   return e;
 }
 
+namespace {
+cudaError_t launch_slices(const TcSliceSrc &src, int rows_max, EigWork &w, int k0, int jb, uint8_t *S, int64_t blk,
+                          int *E, int es, int eo, cudaStream_t s) {
+  const int rows = (rows_max + 127) / 128 * 128;
+  if (rows <= 0) return cudaSuccess;
+  PP_KT(KT_HER2K, s, (k_tc_slices<<<dim3(rows / 4, w.B), 128, 0, s>>>(src, w.nvec, k0, jb, S, w.sTcS, blk, E, w.sTcE,
+                                                                      es, eo)));
+  count_launch(1);
+  return cudaGetLastError();
+}
+}  // namespace
+
+// A(k1:n, k1:n) -= V W^H + W V^H, lower triangle (panel k0 of width jb).
 cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s) {
   const int k1 = k0 + jb;
   const int mmax = w.nmax - k1;
   if (mmax <= 0) return cudaSuccess;
+  const int64_t sW = (int64_t)w.lda * w.nb;
+  const zdf *A = (const zdf *)w.A;
+  // V rows (block part 0) and W rows (block part 1) of the trailing block
+  PP_CUDA_TRY(launch_slices(TcSliceSrc{A + w.lda * k0, w.sA, 1, w.lda, k1, 0, 1, 0}, mmax, w, k0, jb, w.tcS,
+                            TC_RBLK, w.tcE, 2, 0, s));
+  PP_CUDA_TRY(launch_slices(TcSliceSrc{(const zdf *)w.W, sW, 1, w.lda, k1, 0, 0, 0}, mmax, w, k0, jb,
+                            w.tcS + TC_OP, TC_RBLK, w.tcE, 2, 1, s));
+  TcUpdate u{};
+  u.C = (zdf *)w.A;
+  u.ldc = w.lda;
+  u.sC = w.sA;
+  u.rbase = u.cbase = k1;
+  u.ncols_fixed = 0;
+  u.tri = 1;
+  u.nprod = 2;
+  const TcOperand V{w.tcS, w.sTcS, TC_RBLK, w.tcE, w.sTcE, 2, 0};
+  const TcOperand Wo{w.tcS + TC_OP, w.sTcS, TC_RBLK, w.tcE, w.sTcE, 2, 1};
+  u.x[0] = V;
+  u.y[0] = Wo;
+  u.x[1] = Wo;
+  u.y[1] = V;
   const int nrb = (mmax + 127) / 128;
-  const int rows = nrb * 128;
-  PP_KT(KT_HER2K, s, (k_tc_slices<<<dim3(rows / 4, w.B), 128, 0, s>>>((const zdf *)w.A, w.lda, w.sA, (const zdf *)w.W,
-                                                                      (int64_t)w.lda * w.nb, w.nvec, k0, jb, w.tcS,
-                                                                      w.sTcS, w.tcE, w.sTcE)));
   const int nq = (4 * nrb + TC_CB - 1) / TC_CB;
-  PP_KT(KT_HER2K, s, (k_her2k_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>((zdf *)w.A, w.lda, w.sA, w.tcS, w.sTcS,
-                                                                          w.tcE, w.sTcE, w.nvec, k0, jb, w.tcErr)));
-  count_launch(2);
+  PP_KT(KT_HER2K, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>(u, w.nvec, w.tcErr)));
+  count_launch(1);
+  return cudaGetLastError();
+}
+
+// X(k0+1:n, 0:ncols) -= V Y with V the Householder vectors of panel k0 (width
+// jb) and Y (jb x ncols) at Yb[a ldy + c]: the update of the compact-WY
+// back-transform as X Y'^H with Y'(c, a) = conj(Y(a, c)).
+cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t sX, const zdf *Yb, int64_t ldy,
+                      int64_t sY, int ncols, cudaStream_t s) {
+  const int r1 = k0 + 1;
+  const int mmax = w.nmax - r1;
+  if (mmax <= 0 || ncols <= 0) return cudaSuccess;
+  const zdf *A = (const zdf *)w.A;
+  const int64_t vbl = (int64_t)((w.nmax + 127) / 128) * TC_OP;  // the Y' slices follow the V slices
+  const int64_t yexp = (w.nmax + 127) / 128 * 128;
+  PP_CUDA_TRY(launch_slices(TcSliceSrc{A + w.lda * k0, w.sA, 1, w.lda, r1, 0, 1, 0}, mmax, w, k0, jb, w.tcS, TC_OP,
+                            w.tcE, 1, 0, s));
+  PP_CUDA_TRY(launch_slices(TcSliceSrc{Yb, sY, 1, ldy, 0, ncols, 0, 1}, ncols, w, k0, jb, w.tcS + vbl, TC_OP,
+                            w.tcE + yexp, 1, 0, s));
+  TcUpdate u{};
+  u.C = X;
+  u.ldc = ldx;
+  u.sC = sX;
+  u.rbase = r1;
+  u.cbase = 0;
+  u.ncols_fixed = ncols;
+  u.tri = 0;
+  u.nprod = 1;
+  u.x[0] = TcOperand{w.tcS, w.sTcS, TC_OP, w.tcE, w.sTcE, 1, 0};
+  u.y[0] = TcOperand{w.tcS + vbl, w.sTcS, TC_OP, w.tcE + yexp, w.sTcE, 1, 0};
+  u.x[1] = u.x[0];
+  u.y[1] = u.y[0];
+  const int nrb = (mmax + 127) / 128;
+  const int nq = ((ncols + 31) / 32 + TC_CB - 1) / TC_CB;
+  PP_KT(KT_APPLYV, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>(u, w.nvec, w.tcErr)));
+  count_launch(1);
   return cudaGetLastError();
 }
 
