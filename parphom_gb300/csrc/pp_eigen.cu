@@ -16,7 +16,8 @@
 //     2 ulp max(|lo|,|hi|)).  Always FP64.
 //  3. Eigenvectors of T by inverse iteration with partial-pivoting LU of
 //     T - lambda I, one thread per eigenvalue cluster, modified Gram-Schmidt
-//     inside clusters (consecutive eigenvalues closer than 1e-7 ||T||).
+//     inside clusters (consecutive eigenvalues closer than 1e-7 ||T||), then
+//     a Gram-Schmidt pass over looser clusters (closer than 1e-5 ||T||).
 //     Always FP64.
 //  4. Back-transform E = Q Z, panel by panel from the last, with the compact
 //     WY form I - V Tf V^H (zlarft forward/columnwise).
@@ -222,11 +223,11 @@ constexpr int HL_T = 32;
 constexpr int HL_LD = HL_T + 1;  // padded column stride of the shared tile
 constexpr int HL_NT = 128;
 template <class R>
-__global__ void __launch_bounds__(HL_NT) k_hemv_lower(const C<R> *Ab, int64_t lda, int64_t sA, const int *nvec,
+__global__ void __launch_bounds__(HL_NT, 11) k_hemv_lower(const C<R> *Ab, int64_t lda, int64_t sA, const int *nvec,
                                                       int i, C<R> *Pb, int64_t sP, int64_t ldp) {
   __shared__ C<R> tile[HL_T * HL_LD];  // tile[c * HL_LD + r]
   __shared__ C<R> vR[HL_T], vC[HL_T];
-  __shared__ C<R> red[4][HL_T];
+  __shared__ C<R> red[2][2][HL_T];
   const int b = blockIdx.z;
   const int n = nvec[b];
   const int r0 = i + 1;
@@ -253,38 +254,38 @@ __global__ void __launch_bounds__(HL_NT) k_hemv_lower(const C<R> *Ab, int64_t ld
     tile[c * HL_LD + r] = (rr < n && cc < n) ? A[rr + lda * cc] : cz<R>();
   }
   __syncthreads();
-  const int lane = tid & (HL_T - 1), part = tid / HL_T;
-  constexpr int SPAN = HL_T / (HL_NT / HL_T);
+  // warps 0-1: A_RC v_C (thread = row, half of the columns each);
+  // warps 2-3: A_RC^H v_R (thread = column, half of the rows each)
+  const int lane = tid & (HL_T - 1), wid = tid / HL_T;
+  const int prod = wid >> 1, half = wid & 1;
+  constexpr int SPAN = HL_T / 2;
   const bool diag = (Rt == Ct);
-  {
+  if (prod == 0) {
     C<R> acc = cz<R>();
     const int r = lane;
+    if (!diag) {
 #pragma unroll
-    for (int c = part * SPAN; c < part * SPAN + SPAN; ++c) {
-      const C<R> a = (!diag || r >= c) ? tile[c * HL_LD + r] : cconj(tile[r * HL_LD + c]);
-      cmac(acc, a, vC[c]);
+      for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) cmac(acc, tile[c * HL_LD + r], vC[c]);
+    } else {  // diagonal tile: the upper part is the conjugate of the mirrored element
+#pragma unroll
+      for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) {
+        const C<R> a = (r >= c) ? tile[c * HL_LD + r] : cconj(tile[r * HL_LD + c]);
+        cmac(acc, a, vC[c]);
+      }
     }
-    red[part][r] = cfin(acc);
-  }
-  __syncthreads();
-  if (part == 0 && rt0 + lane < n) {
-    C<R> s = cadd(cadd(red[0][lane], red[1][lane]), cadd(red[2][lane], red[3][lane]));
-    Pb[b * sP + (int64_t)Ct * ldp + rt0 + lane] = s;
-  }
-  if (diag) return;
-  __syncthreads();
-  {
+    red[0][half][r] = cfin(acc);
+  } else if (!diag) {
     C<R> acc = cz<R>();
     const int c = lane;
 #pragma unroll
-    for (int r = part * SPAN; r < part * SPAN + SPAN; ++r) cmacc(acc, tile[c * HL_LD + r], vR[r]);
-    red[part][c] = cfin(acc);
+    for (int r = half * SPAN; r < half * SPAN + SPAN; ++r) cmacc(acc, tile[c * HL_LD + r], vR[r]);
+    red[1][half][c] = cfin(acc);
   }
   __syncthreads();
-  if (part == 0 && ct0 + lane < n) {
-    C<R> s = cadd(cadd(red[0][lane], red[1][lane]), cadd(red[2][lane], red[3][lane]));
-    Pb[b * sP + (int64_t)Rt * ldp + ct0 + lane] = s;
-  }
+  if (wid == 0 && rt0 + lane < n)
+    Pb[b * sP + (int64_t)Ct * ldp + rt0 + lane] = cadd(red[0][0][lane], red[0][1][lane]);
+  if (wid == 2 && !diag && ct0 + lane < n)
+    Pb[b * sP + (int64_t)Rt * ldp + ct0 + lane] = cadd(red[1][0][lane], red[1][1][lane]);
 }
 
 // X[c] = V(:,c)^H v (c < jj), X[jj+c] = W(:,c)^H v, over rows [i+1, n).
@@ -797,13 +798,14 @@ cudaError_t tridiag_eigenvalues(EigWork &w, char range, double vl, double vu, in
 // ===========================================================================
 // Stage 3: eigenvectors of T by inverse iteration
 // ===========================================================================
+// Clusters of consecutive eigenvalues closer than rel * ||T||.
 __global__ void k_clusters(const double *ww, int64_t sd, const int64_t *rng, const double *tinfo, int *cls,
-                           int64_t scl, int *ncl) {
+                           int64_t scl, int *ncl, double rel) {
   const int b = blockIdx.x;
   if (threadIdx.x != 0) return;
   const int64_t m = rng[b * 8 + 2];
   const double tnorm = tinfo[b * 8 + 2];
-  const double ortol = 1e-7 * tnorm;
+  const double ortol = rel * tnorm;
   const double *w = ww + b * sd;
   int c = 0;
   for (int64_t j = 0; j < m; ++j) {
@@ -811,6 +813,46 @@ __global__ void k_clusters(const double *ww, int64_t sd, const int64_t *rng, con
   }
   cls[b * scl + c] = (int)m;
   ncl[b] = c;
+}
+
+// Inverse iteration orthogonalises only inside tight clusters (where the
+// iterates would otherwise converge to the same vector); eigenvectors of
+// eigenvalues further apart but closer than 1e-5 ||T|| keep an overlap of
+// about eps ||T|| / gap.  One block per matrix removes it by modified
+// Gram-Schmidt inside those loose clusters (block-wide dot products in FP64).
+template <class R>
+__global__ void __launch_bounds__(256) k_reorth(C<R> *Eb, int64_t lde, int64_t sE, const int *nvec, const int *cls,
+                                                int64_t scl, const int *ncl) {
+  __shared__ double red[32];
+  const int b = blockIdx.x;
+  const int n = nvec[b];
+  C<R> *E = Eb + b * sE;
+  const int nc = ncl[b];
+  for (int c = 0; c < nc; ++c) {
+    const int j0 = cls[b * scl + c], j1 = cls[b * scl + c + 1];
+    if (j1 - j0 < 2) continue;
+    for (int j = j0 + 1; j < j1; ++j) {
+      for (int jp = j0; jp < j; ++jp) {
+        double part = 0.0;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) part += RT<R>::to(E[k + lde * jp].re) * RT<R>::to(E[k + lde * j].re);
+        const double dot = block_sum<256>(part, red);
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+          const double v = RT<R>::to(E[k + lde * j].re) - dot * RT<R>::to(E[k + lde * jp].re);
+          E[k + lde * j].re = RT<R>::from(v);
+        }
+        __syncthreads();
+      }
+      double part = 0.0;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double v = RT<R>::to(E[k + lde * j].re);
+        part += v * v;
+      }
+      const double inv = 1.0 / sqrt(block_sum<256>(part, red));
+      for (int k = threadIdx.x; k < n; k += blockDim.x)
+        E[k + lde * j].re = RT<R>::from(RT<R>::to(E[k + lde * j].re) * inv);
+      __syncthreads();
+    }
+  }
 }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
@@ -986,7 +1028,7 @@ template <class R>
 cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
   const int64_t sd = w.nmax;
   const int64_t scl = w.nmax + 1;
-  k_clusters<<<w.B, 32, 0, s>>>(w.w, sd, w.rng, w.tinfo, w.cls, scl, w.ncl);
+  k_clusters<<<w.B, 32, 0, s>>>(w.w, sd, w.rng, w.tinfo, w.cls, scl, w.ncl, 1e-7);
   count_launch(1);
   const int64_t T = w.scratch_threads;
   const int64_t sS = (int64_t)IV_F * w.nmax * T;
@@ -997,6 +1039,9 @@ cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
                                 w.lde, w.sE, w.scratch, w.piv, T, sS, sPv, w.info)));
     count_launch(1);
   }
+  k_clusters<<<w.B, 32, 0, s>>>(w.w, sd, w.rng, w.tinfo, w.cls, scl, w.ncl, 1e-5);
+  PP_KT(KT_INVIT, s, (k_reorth<R><<<w.B, 256, 0, s>>>((C<R> *)w.E, w.lde, w.sE, w.nvec, w.cls, scl, w.ncl)));
+  count_launch(2);
   return cudaGetLastError();
 }
 
