@@ -24,6 +24,7 @@
 // Stages 1 and 4 are templated on the real arithmetic R: double (plain FP64
 // form) or df (double-float on the FP32 pipes, the mixed form).
 #include <atomic>
+#include <algorithm>
 #include <cfloat>
 #include <type_traits>
 #include <cstdio>
@@ -212,80 +213,117 @@ __global__ void __launch_bounds__(TR_NT) k_reflector(C<R> *Ab, int64_t lda, int6
   if (threadIdx.x == 0) A[(i + 1) + lda * i] = cfrom64<R>(1.0, 0.0);
 }
 
-// Lower-triangle Hermitian mat-vec y = A v on the trailing block [i+1, n):
-// one block per lower tile pair (R >= C) of HL_T x HL_T; the tile is read
-// once and gives both A_RC v_C (into slot C of the rows of R) and
-// A_RC^H v_R (into slot R of the rows of C).  Every row receives exactly one
-// partial per slot 0 .. ntiles-1, summed later by k_wcorr.  Small tiles and
-// blocks keep many blocks resident per SM, so tile loads of some blocks
-// overlap the (double-float) arithmetic of others.
+// Lower-triangle Hermitian mat-vec y = A v on the trailing block [i+1, n),
+// over the lower tile pairs (R >= C) of HL_T x HL_T: a tile is read once and
+// gives both A_RC v_C (into slot C of the rows of R) and A_RC^H v_R (into
+// slot R of the rows of C).  Every row receives exactly one partial per slot
+// 0 .. ntiles-1, summed later by k_wcorr.  Blocks are persistent over a
+// strided set of tile pairs with two shared-memory buffers: the next tile
+// (and its two vector pieces) is copied by cp.async while the double-float
+// arithmetic of the current one runs.
 constexpr int HL_T = 32;
 constexpr int HL_LD = HL_T + 1;  // padded column stride of the shared tile
 constexpr int HL_NT = 128;
+constexpr int HL_BPS = 6;        // resident blocks per SM
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void tile_pair(int p, int &Rt, int &Ct) {
+  Rt = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+  while ((Rt + 1) * (Rt + 2) / 2 <= p) ++Rt;
+  while (Rt * (Rt + 1) / 2 > p) --Rt;
+  Ct = p - Rt * (Rt + 1) / 2;
+}
 template <class R>
-__global__ void __launch_bounds__(HL_NT, 11) k_hemv_lower(const C<R> *Ab, int64_t lda, int64_t sA, const int *nvec,
-                                                      int i, C<R> *Pb, int64_t sP, int64_t ldp) {
-  __shared__ C<R> tile[HL_T * HL_LD];  // tile[c * HL_LD + r]
-  __shared__ C<R> vR[HL_T], vC[HL_T];
+__global__ void __launch_bounds__(HL_NT, HL_BPS) k_hemv_lower(const C<R> *Ab, int64_t lda, int64_t sA,
+                                                              const int *nvec, int i, C<R> *Pb, int64_t sP,
+                                                              int64_t ldp) {
+  __shared__ __align__(16) C<R> tile[2][HL_T * HL_LD];  // tile[buf][c * HL_LD + r]
+  __shared__ __align__(16) C<R> vR[2][HL_T], vC[2][HL_T];
   __shared__ C<R> red[2][2][HL_T];
   const int b = blockIdx.z;
   const int n = nvec[b];
   const int r0 = i + 1;
-  const int p = blockIdx.x;
-  int Rt = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
-  while ((Rt + 1) * (Rt + 2) / 2 <= p) ++Rt;
-  while (Rt * (Rt + 1) / 2 > p) --Rt;
-  const int Ct = p - Rt * (Rt + 1) / 2;
-  const int rt0 = r0 + Rt * HL_T, ct0 = r0 + Ct * HL_T;
-  if (rt0 >= n) return;
+  if (r0 >= n) return;
+  const int nt = (n - r0 + HL_T - 1) / HL_T;
+  const int npairs = nt * (nt + 1) / 2;
+  if ((int)blockIdx.x >= npairs) return;
   const C<R> *A = Ab + b * sA;
   const int tid = threadIdx.x;
-  if (tid < HL_T) {
-    const int rr = rt0 + tid;
-    vR[tid] = rr < n ? A[rr + lda * i] : cz<R>();
-  } else if (tid < 2 * HL_T) {
-    const int cc = ct0 + tid - HL_T;
-    vC[tid - HL_T] = cc < n ? A[cc + lda * i] : cz<R>();
-  }
+  // copies of tile pair p into buffer buf (zero outside the matrix)
+  auto issue = [&](int p, int buf) {
+    int Rt, Ct;
+    tile_pair(p, Rt, Ct);
+    const int rt0 = r0 + Rt * HL_T, ct0 = r0 + Ct * HL_T;
 #pragma unroll
-  for (int e = tid; e < HL_T * HL_T; e += HL_NT) {
-    const int c = e / HL_T, r = e % HL_T;
-    const int rr = rt0 + r, cc = ct0 + c;
-    tile[c * HL_LD + r] = (rr < n && cc < n) ? A[rr + lda * cc] : cz<R>();
-  }
-  __syncthreads();
+    for (int e = tid; e < HL_T * HL_T; e += HL_NT) {
+      const int c = e / HL_T, r = e % HL_T;
+      const int rr = rt0 + r, cc = ct0 + c;
+      const bool ok = rr < n && cc < n;
+      cp_async16(&tile[buf][c * HL_LD + r], ok ? (const void *)&A[rr + lda * cc] : (const void *)A, ok);
+    }
+    if (tid < HL_T) {
+      const int rr = rt0 + tid;
+      cp_async16(&vR[buf][tid], rr < n ? (const void *)&A[rr + lda * i] : (const void *)A, rr < n);
+    } else if (tid < 2 * HL_T) {
+      const int cc = ct0 + tid - HL_T;
+      cp_async16(&vC[buf][tid - HL_T], cc < n ? (const void *)&A[cc + lda * i] : (const void *)A, cc < n);
+    }
+    cp_async_commit();
+  };
   // warps 0-1: A_RC v_C (thread = row, half of the columns each);
   // warps 2-3: A_RC^H v_R (thread = column, half of the rows each)
   const int lane = tid & (HL_T - 1), wid = tid / HL_T;
   const int prod = wid >> 1, half = wid & 1;
   constexpr int SPAN = HL_T / 2;
-  const bool diag = (Rt == Ct);
-  if (prod == 0) {
-    C<R> acc = cz<R>();
-    const int r = lane;
-    if (!diag) {
+  issue(blockIdx.x, 0);
+  int buf = 0;
+  for (int p = blockIdx.x; p < npairs; p += gridDim.x) {
+    if (p + (int)gridDim.x < npairs)
+      issue(p + gridDim.x, buf ^ 1);
+    else
+      cp_async_commit();  // an empty group keeps "all but the newest" meaning this tile
+    cp_async_wait1();
+    __syncthreads();
+    int Rt, Ct;
+    tile_pair(p, Rt, Ct);
+    const int rt0 = r0 + Rt * HL_T, ct0 = r0 + Ct * HL_T;
+    const bool diag = (Rt == Ct);
+    const C<R> *tl = tile[buf];
+    if (prod == 0) {
+      C<R> acc = cz<R>();
+      const int r = lane;
+      if (!diag) {
 #pragma unroll
-      for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) cmac(acc, tile[c * HL_LD + r], vC[c]);
-    } else {  // diagonal tile: the upper part is the conjugate of the mirrored element
+        for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) cmac(acc, tl[c * HL_LD + r], vC[buf][c]);
+      } else {  // diagonal tile: the upper part is the conjugate of the mirrored element
 #pragma unroll
-      for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) {
-        const C<R> a = (r >= c) ? tile[c * HL_LD + r] : cconj(tile[r * HL_LD + c]);
-        cmac(acc, a, vC[c]);
+        for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) {
+          const C<R> a = (r >= c) ? tl[c * HL_LD + r] : cconj(tl[r * HL_LD + c]);
+          cmac(acc, a, vC[buf][c]);
+        }
       }
-    }
-    red[0][half][r] = cfin(acc);
-  } else if (!diag) {
-    C<R> acc = cz<R>();
-    const int c = lane;
+      red[0][half][r] = cfin(acc);
+    } else if (!diag) {
+      C<R> acc = cz<R>();
+      const int c = lane;
 #pragma unroll
-    for (int r = half * SPAN; r < half * SPAN + SPAN; ++r) cmacc(acc, tile[c * HL_LD + r], vR[r]);
-    red[1][half][c] = cfin(acc);
+      for (int r = half * SPAN; r < half * SPAN + SPAN; ++r) cmacc(acc, tl[c * HL_LD + r], vR[buf][r]);
+      red[1][half][c] = cfin(acc);
+    }
+    __syncthreads();
+    if (wid == 0 && rt0 + lane < n)
+      Pb[b * sP + (int64_t)Ct * ldp + rt0 + lane] = cadd(red[0][0][lane], red[0][1][lane]);
+    if (wid == 2 && !diag && ct0 + lane < n)
+      Pb[b * sP + (int64_t)Rt * ldp + ct0 + lane] = cadd(red[1][0][lane], red[1][1][lane]);
+    __syncthreads();  // the buffer and red are free for the next iteration
+    buf ^= 1;
   }
-  __syncthreads();
-  if (wid == 0 && rt0 + lane < n)
-    Pb[b * sP + (int64_t)Ct * ldp + rt0 + lane] = cadd(red[0][0][lane], red[0][1][lane]);
-  if (wid == 2 && !diag && ct0 + lane < n)
-    Pb[b * sP + (int64_t)Rt * ldp + ct0 + lane] = cadd(red[1][0][lane], red[1][1][lane]);
+  cp_async_wait0();
 }
 
 // X[c] = V(:,c)^H v (c < jj), X[jj+c] = W(:,c)^H v, over rows [i+1, n).
@@ -462,6 +500,18 @@ __global__ void __launch_bounds__(256) k_her2k(C<R> *Ab, int64_t lda, int64_t sA
     }
 }
 
+// Persistent hemv blocks: HL_BPS per SM.
+static int hemv_blocks() {
+  static int v = 0;
+  if (!v) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    v = std::max(1, sms) * HL_BPS;
+  }
+  return v;
+}
+
 template <class R>
 cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
   C<R> *A = (C<R> *)w.A;
@@ -489,8 +539,8 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
       PP_KT(KT_REFL, s, (k_reflector<R><<<B, TR_NT, 0, s>>>(A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal)));
       const int m = nmax - i - 1;
       const int nt = cdiv(m, HL_T);
-      PP_KT(KT_HEMV, s, (k_hemv_lower<R><<<dim3(nt * (nt + 1) / 2, 1, B), HL_NT, 0, s>>>(A, lda, sA, w.nvec, i,
-                                                                                      P, sP, lda)));
+      PP_KT(KT_HEMV, s, (k_hemv_lower<R><<<dim3(std::min(nt * (nt + 1) / 2, hemv_blocks()), 1, B), HL_NT, 0, s>>>(
+                            A, lda, sA, w.nvec, i, P, sP, lda)));
       if (jj > 0) PP_KT(KT_DOTS, s, (k_dots<R><<<dim3(2 * jj, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb)));
       const int nr = cdiv(m, TR_NT);
       const int nrw = cdiv(m, WC_ROWS);
