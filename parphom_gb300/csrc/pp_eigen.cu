@@ -1164,13 +1164,14 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
 template <class R>
 __global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int64_t sWp, const int *nvec,
                                               const int64_t *rng, int k0, int jb, int mode, z64 *G, const z64 *Tf,
-                                              C<R> *Wb, int64_t sWb, int ncol_fixed) {
+                                              C<R> *Wb, int64_t sWb, int ncol_fixed, int nks_fixed = 0) {
   __shared__ C<R> col[32][64];
   __shared__ z64 sT[32][32];
   const int b = blockIdx.y;
   const int n = nvec[b];
   const int ncol = mode == 0 ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
-  const int nks = (n - k0 - 1 + BT_RCH - 1) / BT_RCH;
+  // split-K partials to sum: one per BT_RCH rows, or nks_fixed
+  const int nks = nks_fixed > 0 ? (n - k0 - 1 > 0 ? nks_fixed : 0) : (n - k0 - 1 + BT_RCH - 1) / BT_RCH;
   if (mode != 0) {
     for (int e = threadIdx.x; e < 32 * 32; e += 64) sT[e / 32][e % 32] = Tf[b * 1024 + e];
   }
@@ -1429,12 +1430,18 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
                                                              Wp, 32, sWp, 0, GRAM_RCH)));
     PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(nrows, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, X, ldx, sX, 0, w.nvec,
-                                                                             w.rng, k0, jb, Wp, ldwp, sWp, nrows,
-                                                                             BT_RCH)));
+    const bool tc = std::is_same<R, df>::value && w.tcS && tc_enabled();
+    if (tc) {
+      PP_CUDA_TRY(vhx_tc(w, k0, jb, (const zdf *)X, ldx, sX, nrows, (zdf *)Wp, ldwp, sWp, s));
+    } else {
+      PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(nrows, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, X, ldx, sX, 0, w.nvec,
+                                                                               w.rng, k0, jb, Wp, ldwp, sWp, nrows,
+                                                                               BT_RCH)));
+    }
     PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(nrows, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 2,
-                                                                          w.G, w.Tf, Wb, sWb, nrows)));
-    if (std::is_same<R, df>::value && w.tcS && tc_enabled()) {
+                                                                          w.G, w.Tf, Wb, sWb, nrows,
+                                                                          tc ? vhx_tc_splits(w) : 0)));
+    if (tc) {
       PP_CUDA_TRY(applyV_tc(w, k0, jb, (zdf *)X, ldx, sX, (const zdf *)Wb, ldwp, sWb, nrows, s));
     } else {
       PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(

@@ -142,6 +142,11 @@ cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s);
 // cores: V the Householder vectors of panel k0, Y (jb x ncols) at Yb[a ldy + c].
 cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t sX, const zdf *Yb, int64_t ldy,
                       int64_t sY, int ncols, cudaStream_t s);
+// Wp(a, c) = (V^H X)(a, c) on the tensor cores, split over vhx_tc_splits(w)
+// row ranges into the first split-K slots of Wp.
+int vhx_tc_splits(const EigWork &w);
+cudaError_t vhx_tc(EigWork &w, int k0, int jb, const zdf *X, int64_t ldx, int64_t sX, int ncols, zdf *Wp,
+                   int64_t ldwp, int64_t sWp, cudaStream_t s);
 size_t her2k_tc_bytes(int64_t nmax);
 int64_t her2k_tc_exps(int64_t nmax);
 cudaError_t prepare_her2k_tc();

@@ -26,6 +26,7 @@
 // 28 KB column operands are streamed in by bulk copies, double-buffered so
 // that the next block's copy overlaps this block's MMAs.  One CTA per SM
 // (168 KB of shared memory, 448 tensor-memory columns).
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 #include <cstdlib>
@@ -60,6 +61,7 @@ __device__ __forceinline__ float pow2f(int e) {
 
 // Slices of one operand row held by a warp: lane a has the complex value of
 // panel column a; K index a (real part) and 32 + a (imaginary part).
+template <int TILE = TC_TILE>
 __device__ __forceinline__ int slice_row(zdf x, uint8_t *blk, int row, int lane) {
   float amax = fmaxf(fabsf(x.re.hi), fabsf(x.im.hi));
 #pragma unroll
@@ -71,14 +73,14 @@ __device__ __forceinline__ int slice_row(zdf x, uint8_t *blk, int row, int lane)
     const df v = part ? x.im : x.re;
     const int kk = lane + 32 * part;
     float th = ldexpf(v.hi, -E), tl = ldexpf(v.lo, -E);
-    uint8_t *base = blk + (kk >> 4) * TC_TILE + tc::core_off(row, kk & 15);
+    uint8_t *base = blk + (kk >> 4) * TILE + tc::core_off(row, kk & 15);
 #pragma unroll
     for (int s = 0; s < TC_S; ++s) {
       th = __fmul_rn(th, 256.f);
       tl = __fmul_rn(tl, 256.f);
       const float mi = rintf(th);
       two_sum(__fsub_rn(th, mi), tl, th, tl);
-      *(__nv_bfloat16 *)(base + s * TC_KS * TC_TILE) = __float2bfloat16_rn(mi);
+      *(__nv_bfloat16 *)(base + s * TC_KS * TILE) = __float2bfloat16_rn(mi);
     }
   }
   return E;
@@ -346,6 +348,159 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   if (warp == 0) tc::tmem_dealloc(tm, 512);
 }
 
+// Wp(a, c) = sum_{r > k0} conj(V(r, a)) X(r, c) for the 32 panel columns a
+// and columns c of X (the V^H X of the compact-WY back-transform), on the
+// tensor cores over K = the rows r.  Exact slice products need K <= 64
+// reals, so the rows are taken in chunks of 32: per chunk the X and V rows
+// are sliced in shared memory (grid of the chunk), 224 MMAs accumulate in
+// tensor memory, and the 14 accumulators are folded into double-float
+// registers; the next chunk's rows are loaded into registers while the
+// MMAs run.  CTA = 128 columns c x all 32 a x one of gridDim.y row ranges,
+// whose partial sums go to split-K slots of Wp (blockIdx.y).
+constexpr int VX_STX = 128 * 32 * 16;  // staging of one chunk of X rows (DF)
+constexpr int VX_STV = 32 * 32 * 16;   // and of V rows
+constexpr int VX_SMEM = TC_OP + TC_BBYTES + VX_STX + VX_STV + 128 * 4 + 32 * 4 + 64;
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__global__ void __launch_bounds__(TC_NT, 1) k_vhx_tc(const zdf *Ab, int64_t lda, int64_t sA, const zdf *Xb,
+                                                   int64_t ldx, int64_t sX, const int *nvec, int k0, int jb, int ncols,
+                                                   zdf *Wp, int64_t ldwp, int64_t sWp, int *err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t *sAop = smem;                       // X rows (c), one chunk, sliced
+  uint8_t *sBop = smem + TC_OP;               // V rows (a), one chunk, sliced
+  zdf *stX = (zdf *)(smem + TC_OP + TC_BBYTES);  // stX[c * 32 + row]
+  zdf *stV = (zdf *)(smem + TC_OP + TC_BBYTES + VX_STX);  // stV[a * 32 + row]
+  int *sEc = (int *)(smem + TC_OP + TC_BBYTES + VX_STX + VX_STV);
+  int *sEa = sEc + 128;
+  uint64_t *bar = (uint64_t *)(sEa + 32);
+  uint32_t *tslot = (uint32_t *)(bar + 1);
+  const int b = blockIdx.z;
+  const int n = nvec[b];
+  const int c0 = blockIdx.x * 128;
+  if (c0 >= ncols) return;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int lg = warp & 3, cqt = warp >> 2;
+  const int cl = 32 * lg + lane;  // column of X of this thread (TMEM lane)
+  const int r1 = k0 + 1;
+  const int jmax = min(jb, n - 1 - k0);
+  // this CTA's chunks of 32 rows: [kc_beg, kc_end)
+  const int nck = n > r1 ? (n - r1 + 31) / 32 : 0;
+  const int kc_beg = (int)((int64_t)nck * blockIdx.y / gridDim.y);
+  const int kc_end = (int)((int64_t)nck * (blockIdx.y + 1) / gridDim.y);
+  df accr[TC_CQ], acci[TC_CQ];
+#pragma unroll
+  for (int q = 0; q < TC_CQ; ++q) accr[q] = acci[q] = df{0.f, 0.f};
+  const bool any = kc_beg < kc_end && !*(volatile int *)&err[b];
+  uint32_t tm = 0;
+  if (any) {
+    if (warp == 0) tc::tmem_alloc(tslot, 512);
+    if (tid == 0) {
+      tc::mbar_init(bar, 1);
+      tc::mbar_init_fence();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    tm = *tslot;
+  }
+  const zdf *A = Ab + b * sA;
+  const zdf *X = Xb + b * sX;
+  const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + TC_CQ * cqt;
+  // copies of a chunk into the staging buffers: lane = row, 8 X columns and
+  // 2 V columns per warp (zero outside X, above the panel's unit diagonal
+  // and past jmax)
+  auto load = [&](int kc) {
+    const int r = r1 + 32 * kc + lane;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int c = 8 * warp + j;
+      const bool v = r < n && c0 + c < ncols;
+      cp_async16(&stX[c * 32 + lane], v ? (const void *)&X[r + ldx * (c0 + c)] : (const void *)X, v);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int a = 2 * warp + j;
+      const bool v = r < n && a < jmax && r >= k0 + a + 1;
+      cp_async16(&stV[a * 32 + lane], v ? (const void *)&A[r + lda * (k0 + a)] : (const void *)A, v);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int ok = 1;
+  if (any) load(kc_beg);
+  for (int kc = kc_beg; any && kc < kc_end; ++kc) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+#pragma unroll 1
+    for (int j = 0; j < 8; ++j) {
+      const int e = slice_row(stX[(8 * warp + j) * 32 + lane], sAop, 8 * warp + j, lane);
+      if (lane == 0) sEc[8 * warp + j] = e;
+    }
+#pragma unroll 1
+    for (int j = 0; j < 2; ++j) {
+      const int e = slice_row<1024>(stV[(2 * warp + j) * 32 + lane], sBop, 2 * warp + j, lane);
+      if (lane == 0) sEa[2 * warp + j] = e;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (tid == 0) {
+      tc_issue(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
+      tc::mma_commit(bar);
+    }
+    if (kc + 1 < kc_end) load(kc + 1);  // in flight while the MMAs run
+    const bool done = tc::mbar_wait(bar, (uint32_t)((kc - kc_beg) & 1));
+    ok = __syncthreads_and(done && ok);
+    if (!ok) break;
+    tc::fence_after();
+    const int ec = sEc[cl];
+#pragma unroll
+    for (int cc = 0; cc < TC_CQ / 4; ++cc) {
+      float are[TC_S][4], aim[TC_S][4];
+#pragma unroll
+      for (int uu = 0; uu < TC_S; ++uu) {
+        tc::tmem_ld4(lane_addr + uu * 32 + cc * 4, are[uu]);
+        tc::tmem_ld4(lane_addr + (TC_S + uu) * 32 + cc * 4, aim[uu]);
+      }
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int qq = 0; qq < 4; ++qq) {
+        const int q = 4 * cc + qq;
+        float vr[TC_S], vi[TC_S];
+#pragma unroll
+        for (int uu = 0; uu < TC_S; ++uu) {
+          vr[uu] = are[uu][qq];
+          vi[uu] = aim[uu][qq];
+        }
+        const float sc = pow2f(ec + sEa[TC_CQ * cqt + q] - 16);
+        df pr = combine7(vr), pi = combine7(vi);
+        pr.hi = __fmul_rn(pr.hi, sc);
+        pr.lo = __fmul_rn(pr.lo, sc);
+        pi.hi = __fmul_rn(pi.hi, sc);
+        pi.lo = __fmul_rn(pi.lo, sc);
+        accr[q] = df_add(accr[q], pr);
+        acci[q] = df_add(acci[q], pi);
+      }
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy may land after exit
+  if (any) {
+    if (!ok && tid == 0) atomicExch(&err[b], 1);
+    if (warp == 0) tc::tmem_dealloc(tm, 512);
+  }
+  // split-K slot blockIdx.y of Wp(a, c): this thread's column c, its 8 rows a
+  if (c0 + cl < ncols) {
+    zdf *out = Wp + b * sWp + (int64_t)blockIdx.y * 32 * ldwp;
+#pragma unroll
+    for (int q = 0; q < TC_CQ; ++q) out[(int64_t)(TC_CQ * cqt + q) * ldwp + c0 + cl] = zdf{accr[q], acci[q]};
+  }
+}
+
 }  // namespace
 
 // PARPHOM_GPU_TC=0 selects the CUDA-core trailing update in the double-float
@@ -366,6 +521,7 @@ cudaError_t prepare_her2k_tc() {
   static int done = 0;
   if (done) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(k_cupd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_vhx_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, VX_SMEM);
   if (e == cudaSuccess) done = 1;
   return e;
 }
@@ -446,6 +602,19 @@ cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t s
   const int nrb = (mmax + 127) / 128;
   const int nq = ((ncols + 31) / 32 + TC_CB - 1) / TC_CB;
   PP_KT(KT_APPLYV, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>(u, w.nvec, w.tcErr)));
+  count_launch(1);
+  return cudaGetLastError();
+}
+
+// Wp(a, c) = (V^H X)(a, c) over the rows r > k0 (V: panel k0 of width jb),
+// c < ncols; written to the first split-K slot of Wp.
+int vhx_tc_splits(const EigWork &w) { return std::max(1, std::min(4, w.ksplit)); }
+
+cudaError_t vhx_tc(EigWork &w, int k0, int jb, const zdf *X, int64_t ldx, int64_t sX, int ncols, zdf *Wp,
+                   int64_t ldwp, int64_t sWp, cudaStream_t s) {
+  if (ncols <= 0) return cudaSuccess;
+  PP_KT(KT_VHX, s, (k_vhx_tc<<<dim3((ncols + 127) / 128, vhx_tc_splits(w), w.B), TC_NT, VX_SMEM, s>>>(
+                       (const zdf *)w.A, w.lda, w.sA, X, ldx, sX, w.nvec, k0, jb, ncols, Wp, ldwp, sWp, w.tcErr)));
   count_launch(1);
   return cudaGetLastError();
 }
