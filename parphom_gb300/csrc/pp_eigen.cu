@@ -1450,10 +1450,15 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
     count_launch(6);
   }
   // Eb = X^H Z
-  PP_KT(KT_XHZ, s, (k_xhz<R><<<dim3(cdiv(nrows, XZ_T), cdiv(w.mcap, XZ_T), B), 256, 0, s>>>(
-                       X, ldx, sX, (const C<R> *)w.E, w.lde, w.sE, (C<R> *)w.Eb, (int64_t)w.nbr,
-                       (int64_t)w.nbr * w.mcap, w.nvec, w.rng, nrows)));
-  count_launch(1);
+  if (std::is_same<R, df>::value && w.tcS && tc_enabled()) {
+    PP_CUDA_TRY(xhz_tc(w, (const zdf *)X, ldx, sX, nrows, (const zdf *)w.E, w.lde, w.sE, (zdf *)w.Eb,
+                       (int64_t)w.nbr, (int64_t)w.nbr * w.mcap, s));
+  } else {
+    PP_KT(KT_XHZ, s, (k_xhz<R><<<dim3(cdiv(nrows, XZ_T), cdiv(w.mcap, XZ_T), B), 256, 0, s>>>(
+                         X, ldx, sX, (const C<R> *)w.E, w.lde, w.sE, (C<R> *)w.Eb, (int64_t)w.nbr,
+                         (int64_t)w.nbr * w.mcap, w.nvec, w.rng, nrows)));
+    count_launch(1);
+  }
   return cudaGetLastError();
 }
 

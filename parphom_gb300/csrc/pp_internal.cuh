@@ -145,6 +145,10 @@ cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t s
 // Wp(a, c) = (V^H X)(a, c) on the tensor cores, split over vhx_tc_splits(w)
 // row ranges into the first split-K slots of Wp.
 int vhx_tc_splits(const EigWork &w);
+// Eb(k, j) = sum_r conj(X(r, k)) Z(r, j) on the tensor cores (Z real, stored
+// as complex with zero imaginary part), j < m of each matrix.
+cudaError_t xhz_tc(EigWork &w, const zdf *X, int64_t ldx, int64_t sX, int nrows, const zdf *Z, int64_t ldz,
+                   int64_t sZ, zdf *Eb, int64_t lde, int64_t sE, cudaStream_t s);
 cudaError_t vhx_tc(EigWork &w, int k0, int jb, const zdf *X, int64_t ldx, int64_t sX, int ncols, zdf *Wp,
                    int64_t ldwp, int64_t sWp, cudaStream_t s);
 size_t her2k_tc_bytes(int64_t nmax);

@@ -348,30 +348,73 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   if (warp == 0) tc::tmem_dealloc(tm, 512);
 }
 
-// Wp(a, c) = sum_{r > k0} conj(V(r, a)) X(r, c) for the 32 panel columns a
-// and columns c of X (the V^H X of the compact-WY back-transform), on the
-// tensor cores over K = the rows r.  Exact slice products need K <= 64
-// reals, so the rows are taken in chunks of 32: per chunk the X and V rows
-// are sliced in shared memory (grid of the chunk), 224 MMAs accumulate in
-// tensor memory, and the 14 accumulators are folded into double-float
-// registers; the next chunk's rows are loaded into registers while the
-// MMAs run.  CTA = 128 columns c x all 32 a x one of gridDim.y row ranges,
-// whose partial sums go to split-K slots of Wp (blockIdx.y).
-constexpr int VX_STX = 128 * 32 * 16;  // staging of one chunk of X rows (DF)
-constexpr int VX_STV = 32 * 32 * 16;   // and of V rows
+// Long-K products on the tensor cores, C(c, j) = sum_r A(c, r) conj(B(j, r))
+// with both operands read row-wise from column-major DF matrices (element
+// (c, r) of A at A[r + lda c], conjugated with conj_a; element (j, r) of B at
+// Bm[r + ldb j], real with real_b, zero above a Householder panel's unit
+// diagonal with vmask).  Exact slice products need K <= 64 reals, so the
+// rows r are taken in chunks of 32: per chunk both operands are sliced in
+// shared memory on the grid of the chunk, the MMAs accumulate in tensor
+// memory, and the 14 accumulators are folded into double-float registers;
+// the next chunk's rows are copied (cp.async) while the MMAs run.
+// CTA = 128 rows c x 32 rows j.
+//   mode 0 (V^H X of the back-transform): j = the 32 panel columns, the rows
+//     split over gridDim.y ranges, written to split-K slots of out
+//     (out[(y 32 + j) ldo + c]);
+//   mode 1 (E_b = X^H Z): gridDim.y tiles of j < m_b, all rows, written to
+//     out[c + ldo j].
+struct LongK {
+  const zdf *A;
+  int64_t lda, sA;
+  int conj_a;
+  const zdf *Bm;
+  int64_t ldb, sB;
+  int vmask, real_b;
+  int k0, jb;          // vmask: panel k0 of width jb
+  int rbeg;            // rows [rbeg, n_b)
+  int ncols_a;         // rows c < ncols_a
+  const int64_t *rng;  // mode 1: rows j < rng[8 b + 2]
+  zdf *out;
+  int64_t ldo, sO;
+  int mode;
+};
+constexpr int VX_LD = 33;              // staging row stride (16-byte elements)
+constexpr int VX_STX = 128 * VX_LD * 16;
+constexpr int VX_STV = 32 * VX_LD * 16;
 constexpr int VX_SMEM = TC_OP + TC_BBYTES + VX_STX + VX_STV + 128 * 4 + 32 * 4 + 64;
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
   const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
 }
-__global__ void __launch_bounds__(TC_NT, 1) k_vhx_tc(const zdf *Ab, int64_t lda, int64_t sA, const zdf *Xb,
-                                                   int64_t ldx, int64_t sX, const int *nvec, int k0, int jb, int ncols,
-                                                   zdf *Wp, int64_t ldwp, int64_t sWp, int *err) {
+
+// tc_issue for a real column operand: its imaginary k-steps are zero, so the
+// re accumulator needs row k-steps 0-1 only and the im accumulator 2-3.
+__device__ __forceinline__ void tc_issue_realb(uint32_t tm, uint32_t sa, uint32_t sb) {
+  const uint64_t a0 = tc::sdesc(sa, 128, 256), b0 = tc::sdesc(sb, 128, 256);
+#pragma unroll
+  for (int u = 0; u < TC_S; ++u) {
+#pragma unroll
+    for (int s = 0; s <= u; ++s) {
+      const int t = u - s;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const uint32_t acc = (s == 0 && j == 0) ? 0u : 1u;
+        const uint64_t ar = a0 + (uint64_t)((s * TC_KS + j) * (TC_TILE >> 4));
+        const uint64_t ai = a0 + (uint64_t)((s * TC_KS + j + 2) * (TC_TILE >> 4));
+        const uint64_t br = b0 + (uint64_t)((t * TC_KS + j) * (1024 >> 4));
+        tc::mma_bf16(tm + u * 32, ar, br, TC_ID, acc);
+        tc::mma_bf16(tm + (TC_S + u) * 32, ai, br, TC_ID, acc);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *sAop = smem;                       // X rows (c), one chunk, sliced
-  uint8_t *sBop = smem + TC_OP;               // V rows (a), one chunk, sliced
-  zdf *stX = (zdf *)(smem + TC_OP + TC_BBYTES);  // stX[c * 32 + row]
-  zdf *stV = (zdf *)(smem + TC_OP + TC_BBYTES + VX_STX);  // stV[a * 32 + row]
+  uint8_t *sAop = smem;                                         // A rows (c), one chunk, sliced
+  uint8_t *sBop = smem + TC_OP;                                 // B rows (j), one chunk, sliced
+  zdf *stX = (zdf *)(smem + TC_OP + TC_BBYTES);                 // stX[c * VX_LD + row]
+  zdf *stV = (zdf *)(smem + TC_OP + TC_BBYTES + VX_STX);        // stV[j * VX_LD + row]
   int *sEc = (int *)(smem + TC_OP + TC_BBYTES + VX_STX + VX_STV);
   int *sEa = sEc + 128;
   uint64_t *bar = (uint64_t *)(sEa + 32);
@@ -379,16 +422,18 @@ __global__ void __launch_bounds__(TC_NT, 1) k_vhx_tc(const zdf *Ab, int64_t lda,
   const int b = blockIdx.z;
   const int n = nvec[b];
   const int c0 = blockIdx.x * 128;
-  if (c0 >= ncols) return;
+  if (c0 >= p.ncols_a) return;
+  const int j0 = p.mode == 1 ? 32 * blockIdx.y : 0;
+  const int nj = p.mode == 1 ? (int)p.rng[b * 8 + 2] : min(p.jb, n - 1 - p.k0);  // valid rows j
+  if (p.mode == 1 && j0 >= nj) return;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int lg = warp & 3, cqt = warp >> 2;
-  const int cl = 32 * lg + lane;  // column of X of this thread (TMEM lane)
-  const int r1 = k0 + 1;
-  const int jmax = min(jb, n - 1 - k0);
-  // this CTA's chunks of 32 rows: [kc_beg, kc_end)
-  const int nck = n > r1 ? (n - r1 + 31) / 32 : 0;
-  const int kc_beg = (int)((int64_t)nck * blockIdx.y / gridDim.y);
-  const int kc_end = (int)((int64_t)nck * (blockIdx.y + 1) / gridDim.y);
+  const int cl = 32 * lg + lane;  // row c of this thread (TMEM lane)
+  // chunks of 32 rows r: [kc_beg, kc_end)
+  const int nck = n > p.rbeg ? (n - p.rbeg + 31) / 32 : 0;
+  const int ns = p.mode == 0 ? gridDim.y : 1, si = p.mode == 0 ? blockIdx.y : 0;
+  const int kc_beg = (int)((int64_t)nck * si / ns);
+  const int kc_end = (int)((int64_t)nck * (si + 1) / ns);
   df accr[TC_CQ], acci[TC_CQ];
 #pragma unroll
   for (int q = 0; q < TC_CQ; ++q) accr[q] = acci[q] = df{0.f, 0.f};
@@ -405,25 +450,25 @@ __global__ void __launch_bounds__(TC_NT, 1) k_vhx_tc(const zdf *Ab, int64_t lda,
     tc::fence_after();
     tm = *tslot;
   }
-  const zdf *A = Ab + b * sA;
-  const zdf *X = Xb + b * sX;
+  const zdf *A = p.A + b * p.sA;
+  const zdf *Bm = p.Bm + b * p.sB;
   const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + TC_CQ * cqt;
-  // copies of a chunk into the staging buffers: lane = row, 8 X columns and
-  // 2 V columns per warp (zero outside X, above the panel's unit diagonal
-  // and past jmax)
+  // copies of a chunk into the staging buffers: lane = row r, 8 A rows and 2
+  // B rows per warp (zero outside the operands)
   auto load = [&](int kc) {
-    const int r = r1 + 32 * kc + lane;
+    const int r = p.rbeg + 32 * kc + lane;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int c = 8 * warp + j;
-      const bool v = r < n && c0 + c < ncols;
-      cp_async16(&stX[c * 32 + lane], v ? (const void *)&X[r + ldx * (c0 + c)] : (const void *)X, v);
+    for (int jj = 0; jj < 8; ++jj) {
+      const int c = 8 * warp + jj;
+      const bool v = r < n && c0 + c < p.ncols_a;
+      cp_async16(&stX[c * VX_LD + lane], v ? (const void *)&A[r + p.lda * (c0 + c)] : (const void *)A, v);
     }
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int a = 2 * warp + j;
-      const bool v = r < n && a < jmax && r >= k0 + a + 1;
-      cp_async16(&stV[a * 32 + lane], v ? (const void *)&A[r + lda * (k0 + a)] : (const void *)A, v);
+    for (int jj = 0; jj < 2; ++jj) {
+      const int j = 2 * warp + jj;
+      bool v = r < n && j0 + j < nj;
+      if (p.vmask) v = v && r >= p.k0 + j + 1;
+      cp_async16(&stV[j * VX_LD + lane], v ? (const void *)&Bm[r + p.ldb * (j0 + j)] : (const void *)Bm, v);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
@@ -433,21 +478,28 @@ __global__ void __launch_bounds__(TC_NT, 1) k_vhx_tc(const zdf *Ab, int64_t lda,
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
 #pragma unroll 1
-    for (int j = 0; j < 8; ++j) {
-      const int e = slice_row(stX[(8 * warp + j) * 32 + lane], sAop, 8 * warp + j, lane);
-      if (lane == 0) sEc[8 * warp + j] = e;
+    for (int jj = 0; jj < 8; ++jj) {
+      zdf v = stX[(8 * warp + jj) * VX_LD + lane];
+      if (p.conj_a) v.im = df_neg(v.im);
+      const int e = slice_row(v, sAop, 8 * warp + jj, lane);
+      if (lane == 0) sEc[8 * warp + jj] = e;
     }
 #pragma unroll 1
-    for (int j = 0; j < 2; ++j) {
-      const int e = slice_row<1024>(stV[(2 * warp + j) * 32 + lane], sBop, 2 * warp + j, lane);
-      if (lane == 0) sEa[2 * warp + j] = e;
+    for (int jj = 0; jj < 2; ++jj) {
+      zdf v = stV[(2 * warp + jj) * VX_LD + lane];
+      if (p.real_b) v.im = df{0.f, 0.f};
+      const int e = slice_row<1024>(v, sBop, 2 * warp + jj, lane);
+      if (lane == 0) sEa[2 * warp + jj] = e;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     if (tid == 0) {
-      tc_issue(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
+      if (p.real_b)
+        tc_issue_realb(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
+      else
+        tc_issue(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
       tc::mma_commit(bar);
     }
     if (kc + 1 < kc_end) load(kc + 1);  // in flight while the MMAs run
@@ -493,11 +545,17 @@ __global__ void __launch_bounds__(TC_NT, 1) k_vhx_tc(const zdf *Ab, int64_t lda,
     if (!ok && tid == 0) atomicExch(&err[b], 1);
     if (warp == 0) tc::tmem_dealloc(tm, 512);
   }
-  // split-K slot blockIdx.y of Wp(a, c): this thread's column c, its 8 rows a
-  if (c0 + cl < ncols) {
-    zdf *out = Wp + b * sWp + (int64_t)blockIdx.y * 32 * ldwp;
+  // this thread's row c and its 8 rows j
+  if (c0 + cl < p.ncols_a) {
+    zdf *out = p.out + b * p.sO;
 #pragma unroll
-    for (int q = 0; q < TC_CQ; ++q) out[(int64_t)(TC_CQ * cqt + q) * ldwp + c0 + cl] = zdf{accr[q], acci[q]};
+    for (int q = 0; q < TC_CQ; ++q) {
+      const int j = TC_CQ * cqt + q;
+      if (p.mode == 0)
+        out[((int64_t)blockIdx.y * 32 + j) * p.ldo + c0 + cl] = zdf{accr[q], acci[q]};
+      else if (j0 + j < nj)
+        out[c0 + cl + p.ldo * (int64_t)(j0 + j)] = zdf{accr[q], acci[q]};
+    }
   }
 }
 
@@ -521,7 +579,7 @@ cudaError_t prepare_her2k_tc() {
   static int done = 0;
   if (done) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(k_cupd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_vhx_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, VX_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_longk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, VX_SMEM);
   if (e == cudaSuccess) done = 1;
   return e;
 }
@@ -613,8 +671,49 @@ int vhx_tc_splits(const EigWork &w) { return std::max(1, std::min(4, w.ksplit));
 cudaError_t vhx_tc(EigWork &w, int k0, int jb, const zdf *X, int64_t ldx, int64_t sX, int ncols, zdf *Wp,
                    int64_t ldwp, int64_t sWp, cudaStream_t s) {
   if (ncols <= 0) return cudaSuccess;
-  PP_KT(KT_VHX, s, (k_vhx_tc<<<dim3((ncols + 127) / 128, vhx_tc_splits(w), w.B), TC_NT, VX_SMEM, s>>>(
-                       (const zdf *)w.A, w.lda, w.sA, X, ldx, sX, w.nvec, k0, jb, ncols, Wp, ldwp, sWp, w.tcErr)));
+  LongK p{};
+  p.A = X;
+  p.lda = ldx;
+  p.sA = sX;
+  p.Bm = (const zdf *)w.A + w.lda * k0;
+  p.ldb = w.lda;
+  p.sB = w.sA;
+  p.vmask = 1;
+  p.k0 = k0;
+  p.jb = jb;
+  p.rbeg = k0 + 1;
+  p.ncols_a = ncols;
+  p.out = Wp;
+  p.ldo = ldwp;
+  p.sO = sWp;
+  p.mode = 0;
+  PP_KT(KT_VHX, s, (k_longk_tc<<<dim3((ncols + 127) / 128, vhx_tc_splits(w), w.B), TC_NT, VX_SMEM, s>>>(
+                       p, w.nvec, w.tcErr)));
+  count_launch(1);
+  return cudaGetLastError();
+}
+
+cudaError_t xhz_tc(EigWork &w, const zdf *X, int64_t ldx, int64_t sX, int nrows, const zdf *Z, int64_t ldz,
+                   int64_t sZ, zdf *Eb, int64_t lde, int64_t sE, cudaStream_t s) {
+  if (nrows <= 0) return cudaSuccess;
+  LongK p{};
+  p.A = X;
+  p.lda = ldx;
+  p.sA = sX;
+  p.conj_a = 1;
+  p.Bm = Z;
+  p.ldb = ldz;
+  p.sB = sZ;
+  p.real_b = 1;
+  p.rbeg = 0;
+  p.ncols_a = nrows;
+  p.rng = w.rng;
+  p.out = Eb;
+  p.ldo = lde;
+  p.sO = sE;
+  p.mode = 1;
+  PP_KT(KT_XHZ, s, (k_longk_tc<<<dim3((nrows + 127) / 128, (w.mcap + 31) / 32, w.B), TC_NT, VX_SMEM, s>>>(
+                       p, w.nvec, w.tcErr)));
   count_launch(1);
   return cudaGetLastError();
 }
