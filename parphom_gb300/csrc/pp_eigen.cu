@@ -78,6 +78,24 @@ __device__ z64 block_sum_z(z64 v, double *sh) {
 constexpr int TR_NT = 256;   // threads of the column kernels
 constexpr int HV_CC = 32;    // hemv tile width = rows per partial-sum slot
 
+// Sum of a value over groups of TPR consecutive lanes (every lane of the
+// warp takes part; the group's sum ends up in each of its lanes).
+template <class R, int TPR>
+__device__ __forceinline__ C<R> row_reduce(C<R> y) {
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) {
+    C<R> other;
+    float *dst = (float *)&other;
+    const float *src = (const float *)&y;
+#pragma unroll
+    for (int f = 0; f < (int)(sizeof(C<R>) / sizeof(float)); ++f) dst[f] = __shfl_xor_sync(0xffffffffu, src[f], o);
+    y = cadd(y, other);
+  }
+  return y;
+}
+constexpr int CU_TPR = 8;                // threads per row of k_colupd
+constexpr int CU_ROWS = TR_NT / CU_TPR;  // rows per k_colupd block
+
 // A(i:n,i) -= V(i:n,0:jj) conj(W(i,0:jj))^T + W(i:n,0:jj) conj(V(i,0:jj))^T ;
 // d[i] = Re A(i,i) ; partial sums of |A(r,i)|^2 for r >= i+2.
 // With fin != 0 it first completes the previous panel column jj-1 (the
@@ -88,7 +106,7 @@ constexpr int HV_CC = 32;    // hemv tile width = rows per partial-sum slot
 template <class R>
 __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
                                                   const int *nvec, int i, int k0, int jj, double *dd, int64_t sd,
-                                                  double *nrm, int nrb, int fin, int nprev, const z64 *scal,
+                                                  double *nrm, int nrb, int fin, int nprev, z64 *scal,
                                                   const z64 *wv) {
   __shared__ C<R> sv[64], sw[64];
   __shared__ double red[32];
@@ -99,14 +117,21 @@ __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t
   C<R> *A = Ab + b * sA;
   C<R> *W = Wb + b * sW;
   const int64_t ldw = lda;
-  if (fin && threadIdx.x == 0) {
+  if (fin && threadIdx.x < 32) {  // warp 0 sums the previous column's partials
     z64 sacc{0.0, 0.0};
-    for (int k = 0; k < nprev; ++k) {
+    for (int k = threadIdx.x; k < nprev; k += 32) {
       sacc.re += wv[b * nrb + k].re;
       sacc.im += wv[b * nrb + k].im;
     }
-    const z64 ts = zmul(scal[b * 4 + 1], sacc);
-    s_alpha = z64{-0.5 * ts.re, -0.5 * ts.im};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sacc.re += __shfl_xor_sync(0xffffffffu, sacc.re, o);
+      sacc.im += __shfl_xor_sync(0xffffffffu, sacc.im, o);
+    }
+    if (threadIdx.x == 0) {
+      const z64 ts = zmul(scal[b * 4 + 1], sacc);
+      s_alpha = z64{-0.5 * ts.re, -0.5 * ts.im};
+    }
   }
   __syncthreads();
   const C<R> alpha = fin ? cfrom64<R>(s_alpha) : cz<R>();
@@ -114,38 +139,42 @@ __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t
     sv[c] = A[i + lda * (k0 + c)];
     C<R> wc = W[i + ldw * c];
     if (fin && c == jj - 1) {
-      C<R> t = wc;
-      cmac(t, alpha, A[i + lda * (i - 1)]);
-      wc = cfin(t);
+      cmac(wc, alpha, A[i + lda * (i - 1)]);
+      wc = cfin(wc);
     }
     sw[c] = wc;
   }
   __syncthreads();
-  const int r = i + blockIdx.x * TR_NT + threadIdx.x;
+  // CU_TPR threads share one row, each taking the panel columns c = sub mod
+  // CU_TPR, so that the loads of a row are spread over independent threads.
+  const int sub = threadIdx.x % CU_TPR;
+  const int r = i + blockIdx.x * CU_ROWS + threadIdx.x / CU_TPR;
   double part = 0.0;
+  C<R> acc = cz<R>();
   if (r < n) {
-    C<R> wlast = cz<R>();
-    if (fin) {
-      C<R> t = W[r + ldw * (jj - 1)];
-      cmac(t, alpha, A[r + lda * (i - 1)]);
-      wlast = cfin(t);
-      if (r > i) W[r + ldw * (jj - 1)] = wlast;
-    }
-    C<R> a = A[r + lda * i];
-    if (jj > 0) {
-      C<R> acc = cz<R>();
-      for (int c = 0; c < jj; ++c) {
-        const C<R> wrc = (fin && c == jj - 1) ? wlast : W[r + ldw * c];
-        cmac(acc, A[r + lda * (k0 + c)], cconj(sw[c]));
-        cmac(acc, wrc, cconj(sv[c]));
+#pragma unroll 4
+    for (int c = sub; c < jj; c += CU_TPR) {
+      C<R> wrc = W[r + ldw * c];
+      if (fin && c == jj - 1) {
+        cmac(wrc, alpha, A[r + lda * (i - 1)]);
+        wrc = cfin(wrc);
+        if (r > i) W[r + ldw * c] = wrc;
       }
-      a = csub(a, cfin(acc));
+      cmac(acc, A[r + lda * (k0 + c)], cconj(sw[c]));
+      cmac(acc, wrc, cconj(sv[c]));
     }
+  }
+  acc = cfin(acc);
+  acc = row_reduce<R, CU_TPR>(acc);
+  if (r < n && sub == 0) {
+    C<R> a = A[r + lda * i];
+    if (jj > 0) a = csub(a, acc);
     if (r == i) {
       a.im = RT<R>::zero();
       dd[b * sd + i] = RT<R>::to(a.re);
     }
     A[r + lda * i] = a;
+    if (r == i + 1) scal[b * 4 + 2] = cto64(a);  // alpha of k_reflector
     if (r >= i + 2) {
       z64 t = cto64(a);
       part = t.re * t.re + t.im * t.im;
@@ -156,6 +185,10 @@ __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t
 }
 
 // zlarfg on A(i+1:n, i); v := [1, x/(alpha-beta)] written back in place.
+// Every block forms the same scalars (alpha = A(i+1, i) as saved by
+// k_colupd, the norm from the same partial sums in the same order) and
+// scales RF_ROWS rows; block 0 writes the scalars and v(i+1) = 1.
+constexpr int RF_ROWS = 4 * TR_NT;
 template <class R>
 __global__ void __launch_bounds__(TR_NT) k_reflector(C<R> *Ab, int64_t lda, int64_t sA, const int *nvec, int i,
                                                      int nparts, const double *nrm, int nrb, double *ee, z64 *tau,
@@ -163,10 +196,10 @@ __global__ void __launch_bounds__(TR_NT) k_reflector(C<R> *Ab, int64_t lda, int6
   __shared__ double red[32];
   __shared__ z64 s_scale;
   __shared__ int s_skip;
-  const int b = blockIdx.x;
+  const int b = blockIdx.y;
   const int n = nvec[b];
   if (i >= n - 1) {
-    if (threadIdx.x == 0 && i < n) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && i < n) {
       tau[b * sd + i] = z64{0.0, 0.0};
       ee[b * sd + i] = 0.0;
       scal[b * 4 + 0] = z64{0.0, 0.0};
@@ -179,7 +212,7 @@ __global__ void __launch_bounds__(TR_NT) k_reflector(C<R> *Ab, int64_t lda, int6
   for (int k = threadIdx.x; k < nparts; k += blockDim.x) p += nrm[b * nrb + k];
   double xn2 = block_sum<TR_NT>(p, red);
   if (threadIdx.x == 0) {
-    z64 alpha = cto64(A[(i + 1) + lda * i]);
+    const z64 alpha = scal[b * 4 + 2];
     double xnorm = sqrt(xn2);
     z64 t, sc;
     double beta;
@@ -198,19 +231,23 @@ __global__ void __launch_bounds__(TR_NT) k_reflector(C<R> *Ab, int64_t lda, int6
       double den = dr * dr + di * di;
       sc = z64{dr / den, -di / den};
     }
-    ee[b * sd + i] = beta;
-    tau[b * sd + i] = t;
-    scal[b * 4 + 0] = sc;
-    scal[b * 4 + 1] = t;
+    if (blockIdx.x == 0) {
+      ee[b * sd + i] = beta;
+      tau[b * sd + i] = t;
+      scal[b * 4 + 0] = sc;
+      scal[b * 4 + 1] = t;
+    }
     s_scale = sc;
     s_skip = skip;
   }
   __syncthreads();
   const C<R> scR = cfrom64<R>(s_scale);
   if (!s_skip) {
-    for (int r = i + 2 + threadIdx.x; r < n; r += blockDim.x) A[r + lda * i] = cmul(A[r + lda * i], scR);
+    const int rb = i + 2 + blockIdx.x * RF_ROWS, re = min(n, rb + RF_ROWS);
+#pragma unroll
+    for (int r = rb + threadIdx.x; r < re; r += TR_NT) A[r + lda * i] = cmul(A[r + lda * i], scR);
   }
-  if (threadIdx.x == 0) A[(i + 1) + lda * i] = cfrom64<R>(1.0, 0.0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) A[(i + 1) + lda * i] = cfrom64<R>(1.0, 0.0);
 }
 
 // Lower-triangle Hermitian mat-vec y = A v on the trailing block [i+1, n),
@@ -341,6 +378,7 @@ __global__ void __launch_bounds__(TR_NT) k_dots(const C<R> *Ab, int64_t lda, int
   const int c = useW ? c2 - jj : c2;
   const C<R> *Xc = useW ? (W + lda * c) : (A + lda * (k0 + c));
   C<R> acc = cz<R>();
+#pragma unroll 4
   for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) cmacc(acc, Xc[r], A[r + lda * i]);
   z64 s = block_sum_z<TR_NT>(cto64(cfin(acc)), red);
   if (threadIdx.x == 0) X[b * ldx + c2] = s;
@@ -375,27 +413,20 @@ __global__ void __launch_bounds__(TR_NT) k_wcorr(const C<R> *Ab, int64_t lda, in
   const int nch = cdiv_dev(n - i - 1, HV_CC);
   C<R> y = cz<R>();
   if (r < n) {
-    for (int ch = sub; ch < nch; ch += WC_TPR) y = cadd(y, Pb[b * sP + (int64_t)ch * ldp + r]);
-  }
-  // reduce the WC_TPR partial sums of this row (lanes of one warp)
-#pragma unroll
-  for (int o = WC_TPR / 2; o > 0; o >>= 1) {
-    C<R> other;
-    float *dst = (float *)&other;
-    const float *src = (const float *)&y;
-#pragma unroll
-    for (int f = 0; f < (int)(sizeof(C<R>) / sizeof(float)); ++f) dst[f] = __shfl_xor_sync(0xffffffffu, src[f], o);
-    y = cadd(y, other);
-  }
-  if (r < n && sub == 0) {
-    if (jj > 0) {
-      C<R> acc = cz<R>();
-      for (int c = 0; c < jj; ++c) {
-        cmac(acc, W[r + lda * c], x1[c]);
-        cmac(acc, A[r + lda * (k0 + c)], x2[c]);
-      }
-      y = csub(y, cfin(acc));
+    const C<R> *Pr = Pb + b * sP + r;
+#pragma unroll 4
+    for (int ch = sub; ch < nch; ch += WC_TPR) y = cadd(y, Pr[(int64_t)ch * ldp]);
+    // this thread's share of the panel corrections, columns c = sub mod WC_TPR
+    C<R> acc = cz<R>();
+#pragma unroll 4
+    for (int c = sub; c < jj; c += WC_TPR) {
+      cmac(acc, W[r + lda * c], x1[c]);
+      cmac(acc, A[r + lda * (k0 + c)], x2[c]);
     }
+    y = csub(y, cfin(acc));
+  }
+  y = row_reduce<R, WC_TPR>(y);
+  if (r < n && sub == 0) {
     const C<R> t = cfrom64<R>(scal[b * 4 + 1]);
     C<R> w = cmul(t, y);
     W[r + lda * jj] = w;
@@ -526,7 +557,7 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
     int nprev = 0;  // k_wcorr blocks of the previous column, when its w is still to be completed
     for (int jj = 0; jj < jb; ++jj) {
       const int i = k0 + jj;
-      const int nparts = cdiv(nmax - i, TR_NT);
+      const int nparts = cdiv(nmax - i, CU_ROWS);
       const int fin = (jj > 0 && nprev > 0) ? 1 : 0;
       PP_KT(KT_COLUPD, s, (k_colupd<R><<<dim3(nparts, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, w.d, sd,
                                                                          w.nrm, w.nrb, fin, nprev, w.scal,
@@ -536,7 +567,8 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
         count_launch(1);
         continue;
       }
-      PP_KT(KT_REFL, s, (k_reflector<R><<<B, TR_NT, 0, s>>>(A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal)));
+      PP_KT(KT_REFL, s, (k_reflector<R><<<dim3(std::max(1, cdiv(nmax - i - 2, RF_ROWS)), B), TR_NT, 0, s>>>(
+                            A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal)));
       const int m = nmax - i - 1;
       const int nt = cdiv(m, HL_T);
       PP_KT(KT_HEMV, s, (k_hemv_lower<R><<<dim3(std::min(nt * (nt + 1) / 2, hemv_blocks()), 1, B), HL_NT, 0, s>>>(

@@ -53,6 +53,7 @@ constexpr int TC_NACC = 2 * TC_S;                // accumulators: (re, im) x sli
 constexpr uint32_t TC_ID = tc::idesc_bf16(128, 32, 0);
 constexpr uint32_t TC_IDN = tc::idesc_bf16(128, 32, 1);
 static_assert(TC_NACC * 32 <= 512, "accumulators exceed tensor memory");
+static_assert(TC_NT == 4 * 128, "long-K slicing maps one thread to each (row, k-step) of 128 rows");
 
 // 2^e as a float (exact for -126 <= e <= 127)
 __device__ __forceinline__ float pow2f(int e) {
@@ -409,6 +410,59 @@ __device__ __forceinline__ void tc_issue_realb(uint32_t tm, uint32_t sa, uint32_
   }
 }
 
+// Slices of one k-step (16 reals) of an operand row staged in shared memory
+// (strow[r], r < 32: the real parts are K = r, the imaginary parts K = 32 + r),
+// on the same grid as slice_row.  The NKS threads of a row are adjacent lanes
+// (lane % NKS = k-step) and share the row's exponent E (largest magnitude
+// below 2^E).  Each digit is rounded onto its fixed grid without scaling:
+// m = (t + 1.5 2^(23-8(s+1))) - 1.5 2^(23-8(s+1)) is t rounded to a multiple
+// of 2^-8(s+1); t - m is exact, and is either 0 or at least ulp(t) > 2 |tl|,
+// so Fast2Sum keeps the residual pair exact and normalised.  Every thread
+// writes two 16-byte core-matrix rows per slice.
+template <int TILE, int NKS>
+__device__ __forceinline__ int slice_kstep(const zdf *strow, bool neg_im, uint8_t *blk, int row, int ks) {
+  const int part = ks >> 1, rb = (ks & 1) * 16;
+  float th[16], tl[16];
+  float amax = 0.f;
+#pragma unroll
+  for (int t = 0; t < 16; ++t) {
+    const df v = ((const df *)&strow[rb + t])[part];
+    th[t] = v.hi;
+    tl[t] = v.lo;
+    amax = fmaxf(amax, fabsf(v.hi));
+  }
+  amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 1));
+  if (NKS == 4) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 2));
+  int E = 0;
+  if (amax > 0.f) frexpf(amax, &E);
+  const float sc = (part && neg_im) ? -pow2f(-E) : pow2f(-E);
+#pragma unroll
+  for (int t = 0; t < 16; ++t) {
+    th[t] = __fmul_rn(th[t], sc);
+    tl[t] = __fmul_rn(tl[t], sc);
+  }
+  uint8_t *base = blk + ks * TILE + tc::core_off(row, 0);
+#pragma unroll
+  for (int sl = 0; sl < TC_S; ++sl) {
+    const float mag = 1.5f * (float)(1 << 15) * pow2f(-8 * sl);  // 1.5 2^(23 - 8(sl+1))
+    const float up = pow2f(8 * (sl + 1));
+    uint32_t w[8];
+#pragma unroll
+    for (int t = 0; t < 16; t += 2) {
+      const float m0 = __fsub_rn(__fadd_rn(th[t], mag), mag);
+      const float m1 = __fsub_rn(__fadd_rn(th[t + 1], mag), mag);
+      fast_two_sum(__fsub_rn(th[t], m0), tl[t], th[t], tl[t]);
+      fast_two_sum(__fsub_rn(th[t + 1], m1), tl[t + 1], th[t + 1], tl[t + 1]);
+      const __nv_bfloat162 h = __floats2bfloat162_rn(__fmul_rn(m0, up), __fmul_rn(m1, up));
+      w[t >> 1] = *(const uint32_t *)&h;
+    }
+    uint8_t *dst = base + sl * TC_KS * TILE;
+    *(uint4 *)dst = make_uint4(w[0], w[1], w[2], w[3]);
+    *(uint4 *)(dst + 128) = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+  return E;
+}
+
 __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *sAop = smem;                                         // A rows (c), one chunk, sliced
@@ -477,19 +531,21 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
   for (int kc = kc_beg; any && kc < kc_end; ++kc) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
-#pragma unroll 1
-    for (int jj = 0; jj < 8; ++jj) {
-      zdf v = stX[(8 * warp + jj) * VX_LD + lane];
-      if (p.conj_a) v.im = df_neg(v.im);
-      const int e = slice_row(v, sAop, 8 * warp + jj, lane);
-      if (lane == 0) sEc[8 * warp + jj] = e;
+    {  // A: thread = (row c, k-step)
+      const int c = tid >> 2, ks = tid & 3;
+      const int e = slice_kstep<TC_TILE, 4>(&stX[c * VX_LD], p.conj_a != 0, sAop, c, ks);
+      if (ks == 0) sEc[c] = e;
     }
-#pragma unroll 1
-    for (int jj = 0; jj < 2; ++jj) {
-      zdf v = stV[(2 * warp + jj) * VX_LD + lane];
-      if (p.real_b) v.im = df{0.f, 0.f};
-      const int e = slice_row<1024>(v, sBop, 2 * warp + jj, lane);
-      if (lane == 0) sEa[2 * warp + jj] = e;
+    if (p.real_b) {  // B real: its imaginary k-steps are never read
+      if (tid < 64) {
+        const int j = tid >> 1, ks = tid & 1;
+        const int e = slice_kstep<1024, 2>(&stV[j * VX_LD], false, sBop, j, ks);
+        if (ks == 0) sEa[j] = e;
+      }
+    } else if (tid < 128) {
+      const int j = tid >> 2, ks = tid & 3;
+      const int e = slice_kstep<1024, 4>(&stV[j * VX_LD], false, sBop, j, ks);
+      if (ks == 0) sEa[j] = e;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc::fence_before();
