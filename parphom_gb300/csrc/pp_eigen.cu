@@ -262,6 +262,7 @@ constexpr int HL_T = 32;
 constexpr int HL_LD = HL_T + 1;  // padded column stride of the shared tile
 constexpr int HL_NT = 128;
 constexpr int HL_BPS = 6;        // resident blocks per SM
+constexpr int HL_UNROLL = 4;     // inner-loop unrolling (keeps the kernel's code small)
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
   const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
@@ -335,10 +336,10 @@ __global__ void __launch_bounds__(HL_NT, HL_BPS) k_hemv_lower(const C<R> *Ab, in
       C<R> acc = cz<R>();
       const int r = lane;
       if (!diag) {
-#pragma unroll
+#pragma unroll HL_UNROLL
         for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) cmac(acc, tl[c * HL_LD + r], vC[buf][c]);
       } else {  // diagonal tile: the upper part is the conjugate of the mirrored element
-#pragma unroll
+#pragma unroll HL_UNROLL
         for (int c = half * SPAN; c < half * SPAN + SPAN; ++c) {
           const C<R> a = (r >= c) ? tl[c * HL_LD + r] : cconj(tl[r * HL_LD + c]);
           cmac(acc, a, vC[buf][c]);
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(HL_NT, HL_BPS) k_hemv_lower(const C<R> *Ab, in
     } else if (!diag) {
       C<R> acc = cz<R>();
       const int c = lane;
-#pragma unroll
+#pragma unroll HL_UNROLL
       for (int r = half * SPAN; r < half * SPAN + SPAN; ++r) cmacc(acc, tl[c * HL_LD + r], vR[buf][r]);
       red[1][half][c] = cfin(acc);
     }
