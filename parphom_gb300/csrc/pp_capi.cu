@@ -89,6 +89,10 @@ struct pp_ctx {
   double *d_q = nullptr;
   double *d_w = nullptr, *d_z = nullptr, *d_vel = nullptr;
   int64_t *d_m = nullptr, *d_nz = nullptr, *d_info = nullptr;
+  // second stream for the other half of a batch (forked from and joined to
+  // the working stream with events, so that it is captured into the graph)
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // captured CUDA graph of the last batch configuration
   cudaGraphExec_t gexec = nullptr;
   char gkey[160] = {0};
@@ -302,8 +306,6 @@ int check_opts(const pp_ctx *c, const pp_eig_opts *o) {
   return PP_OK;
 }
 
-// Run the pipeline for B q-points already in c->d_q; results left in the
-// EigWork buffers, velocities in c->vraw.
 // The matrices [off, off+cnt) of a batch as a batch of their own (every
 // per-matrix buffer shifted by `off` of its per-matrix stride).
 EigWork view_of(const EigWork &w, int off, int cnt) {
@@ -348,20 +350,17 @@ EigWork view_of(const EigWork &w, int off, int cnt) {
   return v;
 }
 
-int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
-  EigWork &w = c->w;
-  w.B = B;
-  cudaStream_t s = c->stream;
+// Reduction, tridiagonal eigenpairs and back-transform of the matrices of w
+// on stream s.
+int eig_stages(pp_ctx *c, EigWork &w, const pp_eig_opts *o, bool want_z, cudaStream_t s) {
   const int prec = o->precision;
   const bool vecs = o->jobz == 'V' || o->vel;
-  TRY_CUDA(assemble_batch(c->g, c->d_q, B, w.A, w.lda, w.sA, prec == PP_PREC_MIXED ? 1 : 0, s));
   if (prec == PP_PREC_MIXED)
     TRY_CUDA(tridiagonalize<df>(w, s));
   else
     TRY_CUDA(tridiagonalize<double>(w, s));
   TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s,
                                prec == PP_PREC_MIXED));
-  (void)mcap;
   if (vecs) {
     // Velocities without eigenvector output need only the eigenvector rows
     // of atoms in boundary blocks: back-transform those rows only.
@@ -379,14 +378,57 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
       else
         TRY_CUDA(back_transform<double>(w, s));
     }
-    if (o->vel) {
-      if (rows_only)
-        TRY_CUDA(velocities(c->g, c->d_q, B, w.Eb, w.nbr, (int64_t)w.nbr * w.mcap, prec == PP_PREC_MIXED ? 1 : 0,
-                            w.rng, w.mcap, o->vel_method, c->vraw, c->vpart, c->nsplit, c->g.d_rowmap, s));
-      else
-        TRY_CUDA(velocities(c->g, c->d_q, B, w.E, w.lde, w.sE, prec == PP_PREC_MIXED ? 1 : 0, w.rng, w.mcap,
-                            o->vel_method, c->vraw, c->vpart, c->nsplit, nullptr, s));
-    }
+  }
+  return PP_OK;
+}
+
+bool split_enabled() {
+  const char *e = getenv("PARPHOM_GPU_SPLIT");
+  return !(e && e[0] == '0');
+}
+
+// Run the pipeline for B q-points already in c->d_q; results left in the
+// EigWork buffers, velocities in c->vraw.  With B >= 2 the eigen stages of
+// the two halves of the batch run on two streams: their column recurrences
+// are chains of short, latency-bound launches, and each half fills the gaps
+// of the other.  (Not while per-kernel timing is on: its events assume one
+// stream.)
+int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
+  EigWork &w = c->w;
+  w.B = B;
+  cudaStream_t s = c->stream;
+  const int prec = o->precision;
+  TRY_CUDA(assemble_batch(c->g, c->d_q, B, w.A, w.lda, w.sA, prec == PP_PREC_MIXED ? 1 : 0, s));
+  (void)mcap;
+  if (B >= 2 && split_enabled() && !pp::kt_mask) {
+    if (!c->aux) TRY_CUDA(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    if (!c->ev_fork) TRY_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    if (!c->ev_join) TRY_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    const int h = B / 2;
+    EigWork w0 = view_of(w, 0, h), w1 = view_of(w, h, B - h);
+    TRY_CUDA(cudaEventRecord(c->ev_fork, s));
+    TRY_CUDA(cudaStreamWaitEvent(c->aux, c->ev_fork, 0));
+    const int r0 = eig_stages(c, w0, o, want_z, s);
+    const int r1 = eig_stages(c, w1, o, want_z, c->aux);
+    // always join, so that a capture in progress stays well formed
+    const cudaError_t e0 = cudaEventRecord(c->ev_join, c->aux);
+    const cudaError_t e1 = cudaStreamWaitEvent(s, c->ev_join, 0);
+    if (r0) return r0;
+    if (r1) return r1;
+    TRY_CUDA(e0);
+    TRY_CUDA(e1);
+  } else {
+    const int r = eig_stages(c, w, o, want_z, s);
+    if (r) return r;
+  }
+  if (o->vel) {
+    const bool rows_only = !want_z && c->g.nbrows < c->g.n;
+    if (rows_only)
+      TRY_CUDA(velocities(c->g, c->d_q, B, w.Eb, w.nbr, (int64_t)w.nbr * w.mcap, prec == PP_PREC_MIXED ? 1 : 0,
+                          w.rng, w.mcap, o->vel_method, c->vraw, c->vpart, c->nsplit, c->g.d_rowmap, s));
+    else
+      TRY_CUDA(velocities(c->g, c->d_q, B, w.E, w.lde, w.sE, prec == PP_PREC_MIXED ? 1 : 0, w.rng, w.mcap,
+                          o->vel_method, c->vraw, c->vpart, c->nsplit, nullptr, s));
   }
   return PP_OK;
 }
@@ -662,6 +704,12 @@ int pp_ctx_destroy(pp_ctx *c) {
   cudaFree(c->g.d_bndmask);
   cudaFree(c->g.d_brows);
   cudaFree(c->g.d_rowmap);
+  if (c->aux) {
+    cudaStreamSynchronize(c->aux);
+    cudaStreamDestroy(c->aux);
+  }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PP_OK;
