@@ -89,10 +89,11 @@ struct pp_ctx {
   double *d_q = nullptr;
   double *d_w = nullptr, *d_z = nullptr, *d_vel = nullptr;
   int64_t *d_m = nullptr, *d_nz = nullptr, *d_info = nullptr;
-  // second stream for the other half of a batch (forked from and joined to
-  // the working stream with events, so that it is captured into the graph)
-  cudaStream_t aux = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // extra streams for the other parts of a batch (forked from and joined to
+  // the working stream with events, so that they are captured into the graph)
+  static constexpr int MAX_SPLIT = 8;
+  cudaStream_t aux[MAX_SPLIT - 1] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[MAX_SPLIT - 1] = {};
   // captured CUDA graph of the last batch configuration
   cudaGraphExec_t gexec = nullptr;
   char gkey[160] = {0};
@@ -382,16 +383,19 @@ int eig_stages(pp_ctx *c, EigWork &w, const pp_eig_opts *o, bool want_z, cudaStr
   return PP_OK;
 }
 
-bool split_enabled() {
+// Streams a batch is split over (PARPHOM_GPU_SPLIT, 1 .. MAX_SPLIT; default 4).
+int split_ways() {
   const char *e = getenv("PARPHOM_GPU_SPLIT");
-  return !(e && e[0] == '0');
+  if (!e || !e[0]) return 4;
+  const int k = atoi(e);
+  return std::max(1, std::min(k, pp_ctx::MAX_SPLIT));
 }
 
 // Run the pipeline for B q-points already in c->d_q; results left in the
 // EigWork buffers, velocities in c->vraw.  With B >= 2 the eigen stages of
-// the two halves of the batch run on two streams: their column recurrences
-// are chains of short, latency-bound launches, and each half fills the gaps
-// of the other.  (Not while per-kernel timing is on: its events assume one
+// parts of the batch run on separate streams: their column recurrences are
+// chains of short, latency-bound launches, and each part fills the gaps of
+// the others.  (Not while per-kernel timing is on: its events assume one
 // stream.)
 int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   EigWork &w = c->w;
@@ -400,23 +404,32 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   const int prec = o->precision;
   TRY_CUDA(assemble_batch(c->g, c->d_q, B, w.A, w.lda, w.sA, prec == PP_PREC_MIXED ? 1 : 0, s));
   (void)mcap;
-  if (B >= 2 && split_enabled() && !pp::kt_mask) {
-    if (!c->aux) TRY_CUDA(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+  const int ways = pp::kt_mask ? 1 : std::min(B, split_ways());
+  if (ways >= 2) {
     if (!c->ev_fork) TRY_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-    if (!c->ev_join) TRY_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
-    const int h = B / 2;
-    EigWork w0 = view_of(w, 0, h), w1 = view_of(w, h, B - h);
+    for (int k = 0; k < ways - 1; ++k) {
+      if (!c->aux[k]) TRY_CUDA(cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking));
+      if (!c->ev_join[k]) TRY_CUDA(cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming));
+    }
     TRY_CUDA(cudaEventRecord(c->ev_fork, s));
-    TRY_CUDA(cudaStreamWaitEvent(c->aux, c->ev_fork, 0));
-    const int r0 = eig_stages(c, w0, o, want_z, s);
-    const int r1 = eig_stages(c, w1, o, want_z, c->aux);
+    int r = PP_OK;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < ways; ++k) {
+      const int off = (int)((int64_t)B * k / ways), cnt = (int)((int64_t)B * (k + 1) / ways) - off;
+      EigWork v = view_of(w, off, cnt);
+      cudaStream_t sk = k == 0 ? s : c->aux[k - 1];
+      if (k > 0 && e == cudaSuccess) e = cudaStreamWaitEvent(sk, c->ev_fork, 0);
+      const int rk = eig_stages(c, v, o, want_z, sk);
+      if (!r) r = rk;
+    }
     // always join, so that a capture in progress stays well formed
-    const cudaError_t e0 = cudaEventRecord(c->ev_join, c->aux);
-    const cudaError_t e1 = cudaStreamWaitEvent(s, c->ev_join, 0);
-    if (r0) return r0;
-    if (r1) return r1;
-    TRY_CUDA(e0);
-    TRY_CUDA(e1);
+    for (int k = 1; k < ways; ++k) {
+      const cudaError_t ek = cudaEventRecord(c->ev_join[k - 1], c->aux[k - 1]);
+      const cudaError_t ew = cudaStreamWaitEvent(s, c->ev_join[k - 1], 0);
+      if (e == cudaSuccess) e = ek != cudaSuccess ? ek : ew;
+    }
+    if (r) return r;
+    TRY_CUDA(e);
   } else {
     const int r = eig_stages(c, w, o, want_z, s);
     if (r) return r;
@@ -704,12 +717,14 @@ int pp_ctx_destroy(pp_ctx *c) {
   cudaFree(c->g.d_bndmask);
   cudaFree(c->g.d_brows);
   cudaFree(c->g.d_rowmap);
-  if (c->aux) {
-    cudaStreamSynchronize(c->aux);
-    cudaStreamDestroy(c->aux);
+  for (int k = 0; k < pp_ctx::MAX_SPLIT - 1; ++k) {
+    if (c->aux[k]) {
+      cudaStreamSynchronize(c->aux[k]);
+      cudaStreamDestroy(c->aux[k]);
+    }
+    if (c->ev_join[k]) cudaEventDestroy(c->ev_join[k]);
   }
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PP_OK;
