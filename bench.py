@@ -11,7 +11,7 @@ host memory in, frequencies and velocities back to host memory).  Every
 matrix (363 MB per q in double-float complex) is larger than L2, so no L2
 flush is needed between steps.
 
-Also measured: the plain FP64 form on a smaller batch of the same q (the
+Also measured: the plain FP64 form on a batch of the same size (the
 ratio the metric names), the largest frequency difference between the two
 forms, per-kernel CUDA-event times for the roofline, SM clocks during the
 timed region, and the CPU oracle on one q (cpu_baseline).
@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--batch", type=int, default=16, help="q-points per step and rank")
+    p.add_argument("--batch", type=int, default=32, help="q-points per step and rank")
     p.add_argument("--m", type=int, default=11, help="twist index (11 -> N=1588)")
     p.add_argument("--fp64-batch", type=int, default=0, help="q per FP64-form step (0: same as --batch)")
     p.add_argument("--no-cpu-baseline", action="store_true")

@@ -91,7 +91,7 @@ struct pp_ctx {
   int64_t *d_m = nullptr, *d_nz = nullptr, *d_info = nullptr;
   // extra streams for the other parts of a batch (forked from and joined to
   // the working stream with events, so that they are captured into the graph)
-  static constexpr int MAX_SPLIT = 8;
+  static constexpr int MAX_SPLIT = 16;
   cudaStream_t aux[MAX_SPLIT - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[MAX_SPLIT - 1] = {};
   // captured CUDA graph of the last batch configuration
@@ -383,10 +383,10 @@ int eig_stages(pp_ctx *c, EigWork &w, const pp_eig_opts *o, bool want_z, cudaStr
   return PP_OK;
 }
 
-// Streams a batch is split over (PARPHOM_GPU_SPLIT, 1 .. MAX_SPLIT; default 4).
+// Streams a batch is split over (PARPHOM_GPU_SPLIT, 1 .. MAX_SPLIT; default 8).
 int split_ways() {
   const char *e = getenv("PARPHOM_GPU_SPLIT");
-  if (!e || !e[0]) return 4;
+  if (!e || !e[0]) return 8;
   const int k = atoi(e);
   return std::max(1, std::min(k, pp_ctx::MAX_SPLIT));
 }
