@@ -339,9 +339,9 @@ def main():
 
 
 # DRAM bytes (read + write) over algorithmic bytes of one k_hemv_lower launch,
-# measured with ncu --set full at N=1588, batch 4, column 300: 682.6 MB for
-# 637.5 MB (the partial sums written for the w-completion are the 7%).
-HEMV_TRAFFIC_RATIO = 1.071
+# measured with ncu --set full at N=1588, batch 4, column 300: 695.7 MB for
+# 637.5 MB (reads 1.032x; the partial sums written for the w-completion 5.9%).
+HEMV_TRAFFIC_RATIO = 1.091
 
 
 def roofline_for(kclass, rec, n, nq):
@@ -364,7 +364,7 @@ def roofline_for(kclass, rec, n, nq):
                 "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
                 "traffic": HEMV_TRAFFIC_RATIO * byts / launches,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (column 300, "
-                                  "batch 4) = 1.071 x its algorithmic bytes, scaled to this average launch",
+                                  "batch 4) = 1.091 x its algorithmic bytes, scaled to this average launch",
                 "launches": launches, "avg_launch_ms": ms / launches,
                 "algorithmic_bytes_per_launch": byts / launches}
     # FP32-pipe kernels (double-float arithmetic): count complex MACs
