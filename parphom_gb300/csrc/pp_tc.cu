@@ -363,14 +363,20 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
 //     split over gridDim.y ranges, written to split-K slots of out
 //     (out[(y 32 + j) ldo + c]);
 //   mode 1 (E_b = X^H Z): gridDim.y tiles of j < m_b, all rows, written to
-//     out[c + ldo j].
+//     out[c + ldo j];
+//   mode 2 (E_b = X^H Z with the roles swapped): A = Z (real, rows c < m_b:
+//     the eigenvector index), B = X (conjugated, rows j < nrows_b: the
+//     boundary row), written to out[j + ldo c].  A real A operand needs only
+//     its two real k-steps sliced, so a chunk's slicing (128 x 2 + 32 x 4
+//     k-steps) runs in one pass of the CTA's threads.
 struct LongK {
   const zdf *A;
   int64_t lda, sA;
-  int conj_a;
+  int conj_a, real_a;
   const zdf *Bm;
   int64_t ldb, sB;
-  int vmask, real_b;
+  int vmask, real_b, conj_b;
+  int nrows_b;         // mode 2: valid B rows
   int k0, jb;          // vmask: panel k0 of width jb
   int rbeg;            // rows [rbeg, n_b)
   int ncols_a;         // rows c < ncols_a
@@ -463,6 +469,28 @@ __device__ __forceinline__ int slice_kstep(const zdf *strow, bool neg_im, uint8_
   return E;
 }
 
+// tc_issue for a real row operand: re acc pairs row k-step j (j < 2) with
+// column k-step j, im acc the same row k-step with column k-step j + 2.
+__device__ __forceinline__ void tc_issue_reala(uint32_t tm, uint32_t sa, uint32_t sb) {
+  const uint64_t a0 = tc::sdesc(sa, 128, 256), b0 = tc::sdesc(sb, 128, 256);
+#pragma unroll
+  for (int u = 0; u < TC_S; ++u) {
+#pragma unroll
+    for (int s = 0; s <= u; ++s) {
+      const int t = u - s;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const uint32_t acc = (s == 0 && j == 0) ? 0u : 1u;
+        const uint64_t ar = a0 + (uint64_t)((s * TC_KS + j) * (TC_TILE >> 4));
+        const uint64_t br = b0 + (uint64_t)((t * TC_KS + j) * (1024 >> 4));
+        const uint64_t bi = b0 + (uint64_t)((t * TC_KS + j + 2) * (1024 >> 4));
+        tc::mma_bf16(tm + u * 32, ar, br, TC_ID, acc);
+        tc::mma_bf16(tm + (TC_S + u) * 32, ar, bi, TC_ID, acc);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *sAop = smem;                                         // A rows (c), one chunk, sliced
@@ -476,10 +504,11 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
   const int b = blockIdx.z;
   const int n = nvec[b];
   const int c0 = blockIdx.x * 128;
-  if (c0 >= p.ncols_a) return;
-  const int j0 = p.mode == 1 ? 32 * blockIdx.y : 0;
-  const int nj = p.mode == 1 ? (int)p.rng[b * 8 + 2] : min(p.jb, n - 1 - p.k0);  // valid rows j
-  if (p.mode == 1 && j0 >= nj) return;
+  const int na = p.mode == 2 ? (int)p.rng[b * 8 + 2] : p.ncols_a;  // valid rows c
+  if (c0 >= na) return;
+  const int j0 = p.mode >= 1 ? 32 * blockIdx.y : 0;
+  const int nj = p.mode == 1 ? (int)p.rng[b * 8 + 2] : p.mode == 2 ? p.nrows_b : min(p.jb, n - 1 - p.k0);  // valid rows j
+  if (p.mode >= 1 && j0 >= nj) return;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int lg = warp & 3, cqt = warp >> 2;
   const int cl = 32 * lg + lane;  // row c of this thread (TMEM lane)
@@ -514,7 +543,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
 #pragma unroll
     for (int jj = 0; jj < 8; ++jj) {
       const int c = 8 * warp + jj;
-      const bool v = r < n && c0 + c < p.ncols_a;
+      const bool v = r < n && c0 + c < na;
       cp_async16(&stX[c * VX_LD + lane], v ? (const void *)&A[r + p.lda * (c0 + c)] : (const void *)A, v);
     }
 #pragma unroll
@@ -531,28 +560,42 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
   for (int kc = kc_beg; any && kc < kc_end; ++kc) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
-    {  // A: thread = (row c, k-step)
-      const int c = tid >> 2, ks = tid & 3;
-      const int e = slice_kstep<TC_TILE, 4>(&stX[c * VX_LD], p.conj_a != 0, sAop, c, ks);
-      if (ks == 0) sEc[c] = e;
-    }
-    if (p.real_b) {  // B real: its imaginary k-steps are never read
-      if (tid < 64) {
-        const int j = tid >> 1, ks = tid & 1;
-        const int e = slice_kstep<1024, 2>(&stV[j * VX_LD], false, sBop, j, ks);
+    if (p.real_a) {  // A real: threads 0-255 slice its real k-steps, 256-383 slice B
+      if (tid < 256) {
+        const int c = tid >> 1, ks = tid & 1;
+        const int e = slice_kstep<TC_TILE, 2>(&stX[c * VX_LD], false, sAop, c, ks);
+        if (ks == 0) sEc[c] = e;
+      } else if (tid < 384) {
+        const int j = (tid - 256) >> 2, ks = tid & 3;
+        const int e = slice_kstep<1024, 4>(&stV[j * VX_LD], p.conj_b != 0, sBop, j, ks);
         if (ks == 0) sEa[j] = e;
       }
-    } else if (tid < 128) {
-      const int j = tid >> 2, ks = tid & 3;
-      const int e = slice_kstep<1024, 4>(&stV[j * VX_LD], false, sBop, j, ks);
-      if (ks == 0) sEa[j] = e;
+    } else {
+      {  // A: thread = (row c, k-step)
+        const int c = tid >> 2, ks = tid & 3;
+        const int e = slice_kstep<TC_TILE, 4>(&stX[c * VX_LD], p.conj_a != 0, sAop, c, ks);
+        if (ks == 0) sEc[c] = e;
+      }
+      if (p.real_b) {  // B real: its imaginary k-steps are never read
+        if (tid < 64) {
+          const int j = tid >> 1, ks = tid & 1;
+          const int e = slice_kstep<1024, 2>(&stV[j * VX_LD], false, sBop, j, ks);
+          if (ks == 0) sEa[j] = e;
+        }
+      } else if (tid < 128) {
+        const int j = tid >> 2, ks = tid & 3;
+        const int e = slice_kstep<1024, 4>(&stV[j * VX_LD], p.conj_b != 0, sBop, j, ks);
+        if (ks == 0) sEa[j] = e;
+      }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     if (tid == 0) {
-      if (p.real_b)
+      if (p.real_a)
+        tc_issue_reala(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
+      else if (p.real_b)
         tc_issue_realb(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
       else
         tc_issue(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
@@ -602,15 +645,19 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
     if (warp == 0) tc::tmem_dealloc(tm, 512);
   }
   // this thread's row c and its 8 rows j
-  if (c0 + cl < p.ncols_a) {
+  if (c0 + cl < na) {
     zdf *out = p.out + b * p.sO;
 #pragma unroll
     for (int q = 0; q < TC_CQ; ++q) {
       const int j = TC_CQ * cqt + q;
       if (p.mode == 0)
         out[((int64_t)blockIdx.y * 32 + j) * p.ldo + c0 + cl] = zdf{accr[q], acci[q]};
-      else if (j0 + j < nj)
-        out[c0 + cl + p.ldo * (int64_t)(j0 + j)] = zdf{accr[q], acci[q]};
+      else if (j0 + j < nj) {
+        if (p.mode == 1)
+          out[c0 + cl + p.ldo * (int64_t)(j0 + j)] = zdf{accr[q], acci[q]};
+        else
+          out[j0 + j + p.ldo * (int64_t)(c0 + cl)] = zdf{accr[q], acci[q]};
+      }
     }
   }
 }
@@ -753,22 +800,22 @@ cudaError_t xhz_tc(EigWork &w, const zdf *X, int64_t ldx, int64_t sX, int nrows,
                    int64_t sZ, zdf *Eb, int64_t lde, int64_t sE, cudaStream_t s) {
   if (nrows <= 0) return cudaSuccess;
   LongK p{};
-  p.A = X;
-  p.lda = ldx;
-  p.sA = sX;
-  p.conj_a = 1;
-  p.Bm = Z;
-  p.ldb = ldz;
-  p.sB = sZ;
-  p.real_b = 1;
+  p.A = Z;
+  p.lda = ldz;
+  p.sA = sZ;
+  p.real_a = 1;
+  p.Bm = X;
+  p.ldb = ldx;
+  p.sB = sX;
+  p.conj_b = 1;
+  p.nrows_b = nrows;
   p.rbeg = 0;
-  p.ncols_a = nrows;
   p.rng = w.rng;
   p.out = Eb;
   p.ldo = lde;
   p.sO = sE;
-  p.mode = 1;
-  PP_KT(KT_XHZ, s, (k_longk_tc<<<dim3((nrows + 127) / 128, (w.mcap + 31) / 32, w.B), TC_NT, VX_SMEM, s>>>(
+  p.mode = 2;
+  PP_KT(KT_XHZ, s, (k_longk_tc<<<dim3((w.mcap + 127) / 128, (nrows + 31) / 32, w.B), TC_NT, VX_SMEM, s>>>(
                        p, w.nvec, w.tcErr)));
   count_launch(1);
   return cudaGetLastError();
