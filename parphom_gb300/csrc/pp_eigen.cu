@@ -901,17 +901,18 @@ __global__ void k_clusters(const double *ww, int64_t sd, const int64_t *rng, con
 // Inverse iteration orthogonalises only inside tight clusters (where the
 // iterates would otherwise converge to the same vector); eigenvectors of
 // eigenvalues further apart but closer than 1e-5 ||T|| keep an overlap of
-// about eps ||T|| / gap.  One block per matrix removes it by modified
-// Gram-Schmidt inside those loose clusters (block-wide dot products in FP64).
+// about eps ||T|| / gap.  Modified Gram-Schmidt inside those loose clusters
+// removes it, one block per cluster (block-wide dot products in FP64).
+constexpr int RO_BLOCKS = 64;  // blocks per matrix of k_reorth (cluster c goes to block c mod 64)
 template <class R>
 __global__ void __launch_bounds__(256) k_reorth(C<R> *Eb, int64_t lde, int64_t sE, const int *nvec, const int *cls,
                                                 int64_t scl, const int *ncl) {
   __shared__ double red[32];
-  const int b = blockIdx.x;
+  const int b = blockIdx.y;
   const int n = nvec[b];
   C<R> *E = Eb + b * sE;
   const int nc = ncl[b];
-  for (int c = 0; c < nc; ++c) {
+  for (int c = blockIdx.x; c < nc; c += gridDim.x) {  // clusters are independent
     const int j0 = cls[b * scl + c], j1 = cls[b * scl + c + 1];
     if (j1 - j0 < 2) continue;
     for (int j = j0 + 1; j < j1; ++j) {
@@ -997,10 +998,14 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
       const double ck = e[k];
       const double ak1 = d[k + 1] - lam;
       const double bk1 = (k + 1 < n - 1) ? e[k + 1] : 0.0;
-      double u0, u1, u2, l, pn, qn;
+      double u0, u1, u2, l, pn, qn, r0;
       uint8_t sw;
+      // one FP64 division per row (FP64 is the scarce pipe): l from the
+      // pivot's reciprocal, and U is stored with 1/u0 so that the U solves
+      // multiply
       if (fabs(p) >= fabs(ck)) {
-        l = (p == 0.0) ? 0.0 : ck / p;
+        r0 = (p == 0.0) ? 0.0 : 1.0 / p;
+        l = ck * r0;
         u0 = p;
         u1 = qv;
         u2 = 0.0;
@@ -1008,7 +1013,8 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
         qn = bk1;
         sw = 0;
       } else {
-        l = p / ck;
+        r0 = 1.0 / ck;
+        l = p * r0;
         u0 = ck;
         u1 = ak1;
         u2 = bk1;
@@ -1016,7 +1022,7 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
         qn = -l * bk1;
         sw = 1;
       }
-      SU0(k) = (fabs(u0) < pivtol) ? copysign(pivtol, u0) : u0;
+      SU0(k) = (fabs(u0) < pivtol) ? 1.0 / copysign(pivtol, u0) : r0;  // 1 / guarded pivot
       SU1(k) = u1;
       SU2(k) = u2;
       SL(k) = l;
@@ -1024,7 +1030,7 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
       p = pn;
       qv = qn;
     }
-    SU0(n - 1) = (fabs(p) < pivtol) ? copysign(pivtol, p) : p;
+    SU0(n - 1) = 1.0 / ((fabs(p) < pivtol) ? copysign(pivtol, p) : p);
     SU1(n - 1) = 0.0;
     SU2(n - 1) = 0.0;
     // ---- deterministic start vector in (-1, 1)
@@ -1053,7 +1059,7 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
       // U solve
       double y1 = 0.0, y2 = 0.0, amax = 0.0;
       for (int k = n - 1; k >= 0; --k) {
-        const double y = (XS(k) - SU1(k) * y1 - SU2(k) * y2) / SU0(k);
+        const double y = (XS(k) - SU1(k) * y1 - SU2(k) * y2) * SU0(k);
         XS(k) = y;
         amax = fmax(amax, fabs(y));
         y2 = y1;
@@ -1123,7 +1129,7 @@ cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
     count_launch(1);
   }
   k_clusters<<<w.B, 32, 0, s>>>(w.w, sd, w.rng, w.tinfo, w.cls, scl, w.ncl, 1e-5);
-  PP_KT(KT_INVIT, s, (k_reorth<R><<<w.B, 256, 0, s>>>((C<R> *)w.E, w.lde, w.sE, w.nvec, w.cls, scl, w.ncl)));
+  PP_KT(KT_INVIT, s, (k_reorth<R><<<dim3(RO_BLOCKS, w.B), 256, 0, s>>>((C<R> *)w.E, w.lde, w.sE, w.nvec, w.cls, scl, w.ncl)));
   count_launch(2);
   return cudaGetLastError();
 }
