@@ -503,10 +503,13 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
   uint32_t *tslot = (uint32_t *)(bar + 1);
   const int b = blockIdx.z;
   const int n = nvec[b];
-  const int c0 = blockIdx.x * 128;
+  // mode 2 walks the 32-row B tiles fastest (blockIdx.x), so that the CTAs
+  // sharing one 128-row tile of Z run together and read it once from DRAM
+  const int ta = p.mode == 2 ? blockIdx.y : blockIdx.x, tb = p.mode == 2 ? blockIdx.x : blockIdx.y;
+  const int c0 = ta * 128;
   const int na = p.mode == 2 ? (int)p.rng[b * 8 + 2] : p.ncols_a;  // valid rows c
   if (c0 >= na) return;
-  const int j0 = p.mode >= 1 ? 32 * blockIdx.y : 0;
+  const int j0 = p.mode >= 1 ? 32 * tb : 0;
   const int nj = p.mode == 1 ? (int)p.rng[b * 8 + 2] : p.mode == 2 ? p.nrows_b : min(p.jb, n - 1 - p.k0);  // valid rows j
   if (p.mode >= 1 && j0 >= nj) return;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -815,7 +818,7 @@ cudaError_t xhz_tc(EigWork &w, const zdf *X, int64_t ldx, int64_t sX, int nrows,
   p.ldo = lde;
   p.sO = sE;
   p.mode = 2;
-  PP_KT(KT_XHZ, s, (k_longk_tc<<<dim3((w.mcap + 127) / 128, (nrows + 31) / 32, w.B), TC_NT, VX_SMEM, s>>>(
+  PP_KT(KT_XHZ, s, (k_longk_tc<<<dim3((nrows + 31) / 32, (w.mcap + 127) / 128, w.B), TC_NT, VX_SMEM, s>>>(
                        p, w.nvec, w.tcErr)));
   count_launch(1);
   return cudaGetLastError();
