@@ -220,7 +220,8 @@ def main():
     B = args.batch
     dev = torch.device("cuda", local)
     # this rank's q-points: a disjoint slice of the path per rank, cycled
-    q_rank = q_all[rank::world]
+    from parphom_gb300 import replicas
+    q_rank = q_all[replicas.shard(len(q_all), rank, world)]
     nbat = max(1, len(q_rank) // B)
     q_dev = [torch.tensor(np.asfortranarray(np.resize(q_rank[b * B:(b + 1) * B], (B, 3))).ravel(order="F"),
                           dtype=torch.float64, device=dev) for b in range(nbat)]

@@ -13,13 +13,14 @@ cm^-1, `evec` (nz, 3N) compound {r, i} when `compute eigvecs: yes`, and `vel`
 from __future__ import annotations
 
 import argparse
+import contextlib
 import datetime
 import os
 import sys
 
 import numpy as np
 
-from . import api, geometry, hdf5, inputs, synth
+from . import api, geometry, hdf5, inputs, replicas, synth
 
 
 def prepare_force_constants(dset: np.ndarray) -> np.ndarray:
@@ -65,24 +66,36 @@ def run(input_path: str, precision: str = "mixed", batch: int | None = None, qui
         out_path = cfg.output_location + cfg.output_name
         n = 3 * cfg.natom
         B = batch or max(1, min(len(q), 64))
+        # one process per GPU under torchrun: rank r solves q[r::world], rank 0 writes
+        world, rank, local = replicas.world_info()
+        group = None
+        if world > 1:
+            import torch
+            torch.cuda.set_device(local)
+            group = replicas.init_group(world, rank)
+        nmine = len(replicas.shard(len(q), rank, world))
+        who = f"rank {rank}: " if world > 1 else ""
+        done = [0]
         with api.PhononContext(ld.lat, crys, ld.real_pos, ld.masses, ld.at_types, phi) as ctx, \
-                hdf5.Writer(out_path) as wr:
-            for t0 in range(0, len(q), B):
-                qb = q[t0:t0 + B]
+                (hdf5.Writer(out_path) if rank == 0 else contextlib.nullcontext()) as wr:
+
+            def solve(qb):
                 res = ctx.solve(qb, opts, want_z=cfg.compute_eigvecs)
-                for b in range(len(qb)):
-                    t = t0 + b
-                    m = int(res.m[b])
-                    nz = int(res.nz[b])
-                    if res.info[b]:
-                        print(f"q-point {t + 1}: eigensolver info {int(res.info[b])}", file=sys.stderr)
-                    ds = {"q_vec": qb[b], "eigenvalues": res.w[b, :m]}
-                    if cfg.compute_eigvecs and res.z is not None:
-                        ds["evec"] = np.ascontiguousarray(res.z[b][:, :nz].T)
-                    if cfg.group_velocity and res.vel is not None:
-                        ds["vel"] = res.vel[b, :nz]
-                    wr.add_group(f"{t + 1:012d}", ds)
-                _msg(cfg, f"q-points {t0 + 1}-{t0 + len(qb)} of {len(q)} solved (n = {n})")
+                _msg(cfg, f"{who}q-points {done[0] + 1}-{done[0] + len(qb)} of {nmine} solved (n = {n})")
+                done[0] += len(qb)
+                return replicas.split_result(res, len(qb))
+
+            def write(t, r):
+                if r["info"]:
+                    print(f"q-point {t + 1}: eigensolver info {r['info']}", file=sys.stderr)
+                ds = {"q_vec": q[t], "eigenvalues": r["w"]}
+                if cfg.compute_eigvecs and "z" in r:
+                    ds["evec"] = np.ascontiguousarray(r["z"].T)
+                if cfg.group_velocity and "vel" in r:
+                    ds["vel"] = r["vel"]
+                wr.add_group(f"{t + 1:012d}", ds)
+
+            replicas.run_sharded(q, B, solve, write if rank == 0 else None, world, rank, group)
         _msg(cfg, f"Results written to {out_path}")
         return os.path.join(base, out_path)
     finally:
