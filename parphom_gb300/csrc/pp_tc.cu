@@ -349,12 +349,14 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   if (warp == 0) tc::tmem_dealloc(tm, 512);
 }
 
-// Long-K products on the tensor cores, C(c, j) = sum_r A(c, r) conj(B(j, r))
-// with both operands read row-wise from column-major DF matrices (element
-// (c, r) of A at A[r + lda c], conjugated with conj_a; element (j, r) of B at
-// Bm[r + ldb j], real with real_b, zero above a Householder panel's unit
-// diagonal with vmask).  Exact slice products need K <= 64 reals, so the
-// rows r are taken in chunks of 32: per chunk both operands are sliced in
+// Long-K products on the tensor cores over column-major DF matrices read
+// row-wise: element (c, r) of A at A[r + lda c] (conjugated with conj_a),
+// element (j, r) of B at Bm[r + ldb j] (conjugated with conj_b, zero above a
+// Householder panel's unit diagonal with vmask).  A complex A gives
+// C(c, j) = sum_r A(c, r) conj(B(j, r)) (tc_issue forms the conjugate
+// product); a real A (real_a) gives C(c, j) = sum_r A(c, r) B(j, r).
+// Exact slice products need K <= 64 reals, so the rows r are taken in
+// chunks of 32: per chunk both operands are sliced in
 // shared memory on the grid of the chunk, the MMAs accumulate in tensor
 // memory, and the 14 accumulators are folded into double-float registers;
 // the next chunk's rows are copied (cp.async) while the MMAs run.
@@ -362,25 +364,23 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
 //   mode 0 (V^H X of the back-transform): j = the 32 panel columns, the rows
 //     split over gridDim.y ranges, written to split-K slots of out
 //     (out[(y 32 + j) ldo + c]);
-//   mode 1 (E_b = X^H Z): gridDim.y tiles of j < m_b, all rows, written to
-//     out[c + ldo j];
-//   mode 2 (E_b = X^H Z with the roles swapped): A = Z (real, rows c < m_b:
-//     the eigenvector index), B = X (conjugated, rows j < nrows_b: the
-//     boundary row), written to out[j + ldo c].  A real A operand needs only
-//     its two real k-steps sliced, so a chunk's slicing (128 x 2 + 32 x 4
-//     k-steps) runs in one pass of the CTA's threads.
+//   mode 1 (E_b = X^H Z): A = Z (real, rows c < m_b: the eigenvector
+//     index), B = X (conjugated, rows j < nrows_b: the boundary row),
+//     written to out[j + ldo c].  A real A operand needs only its two real
+//     k-steps sliced, so a chunk's slicing (128 x 2 + 32 x 4 k-steps) runs in
+//     one pass of the CTA's threads.
 struct LongK {
   const zdf *A;
   int64_t lda, sA;
   int conj_a, real_a;
   const zdf *Bm;
   int64_t ldb, sB;
-  int vmask, real_b, conj_b;
-  int nrows_b;         // mode 2: valid B rows
+  int vmask, conj_b;
+  int nrows_b;         // mode 1: valid B rows
   int k0, jb;          // vmask: panel k0 of width jb
   int rbeg;            // rows [rbeg, n_b)
   int ncols_a;         // rows c < ncols_a
-  const int64_t *rng;  // mode 1: rows j < rng[8 b + 2]
+  const int64_t *rng;  // mode 1: rows c < rng[8 b + 2]
   zdf *out;
   int64_t ldo, sO;
   int mode;
@@ -392,28 +392,6 @@ constexpr int VX_SMEM = TC_OP + TC_BBYTES + VX_STX + VX_STV + 128 * 4 + 32 * 4 +
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
   const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
-}
-
-// tc_issue for a real column operand: its imaginary k-steps are zero, so the
-// re accumulator needs row k-steps 0-1 only and the im accumulator 2-3.
-__device__ __forceinline__ void tc_issue_realb(uint32_t tm, uint32_t sa, uint32_t sb) {
-  const uint64_t a0 = tc::sdesc(sa, 128, 256), b0 = tc::sdesc(sb, 128, 256);
-#pragma unroll
-  for (int u = 0; u < TC_S; ++u) {
-#pragma unroll
-    for (int s = 0; s <= u; ++s) {
-      const int t = u - s;
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const uint32_t acc = (s == 0 && j == 0) ? 0u : 1u;
-        const uint64_t ar = a0 + (uint64_t)((s * TC_KS + j) * (TC_TILE >> 4));
-        const uint64_t ai = a0 + (uint64_t)((s * TC_KS + j + 2) * (TC_TILE >> 4));
-        const uint64_t br = b0 + (uint64_t)((t * TC_KS + j) * (1024 >> 4));
-        tc::mma_bf16(tm + u * 32, ar, br, TC_ID, acc);
-        tc::mma_bf16(tm + (TC_S + u) * 32, ai, br, TC_ID, acc);
-      }
-    }
-  }
 }
 
 // Slices of one k-step (16 reals) of an operand row staged in shared memory
@@ -503,14 +481,14 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
   uint32_t *tslot = (uint32_t *)(bar + 1);
   const int b = blockIdx.z;
   const int n = nvec[b];
-  // mode 2 walks the 32-row B tiles fastest (blockIdx.x), so that the CTAs
+  // mode 1 walks the 32-row B tiles fastest (blockIdx.x), so that the CTAs
   // sharing one 128-row tile of Z run together and read it once from DRAM
-  const int ta = p.mode == 2 ? blockIdx.y : blockIdx.x, tb = p.mode == 2 ? blockIdx.x : blockIdx.y;
+  const int ta = p.mode == 1 ? blockIdx.y : blockIdx.x, tb = p.mode == 1 ? blockIdx.x : blockIdx.y;
   const int c0 = ta * 128;
-  const int na = p.mode == 2 ? (int)p.rng[b * 8 + 2] : p.ncols_a;  // valid rows c
+  const int na = p.mode == 1 ? (int)p.rng[b * 8 + 2] : p.ncols_a;  // valid rows c
   if (c0 >= na) return;
   const int j0 = p.mode >= 1 ? 32 * tb : 0;
-  const int nj = p.mode == 1 ? (int)p.rng[b * 8 + 2] : p.mode == 2 ? p.nrows_b : min(p.jb, n - 1 - p.k0);  // valid rows j
+  const int nj = p.mode == 1 ? p.nrows_b : min(p.jb, n - 1 - p.k0);  // valid rows j
   if (p.mode >= 1 && j0 >= nj) return;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int lg = warp & 3, cqt = warp >> 2;
@@ -579,13 +557,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
         const int e = slice_kstep<TC_TILE, 4>(&stX[c * VX_LD], p.conj_a != 0, sAop, c, ks);
         if (ks == 0) sEc[c] = e;
       }
-      if (p.real_b) {  // B real: its imaginary k-steps are never read
-        if (tid < 64) {
-          const int j = tid >> 1, ks = tid & 1;
-          const int e = slice_kstep<1024, 2>(&stV[j * VX_LD], false, sBop, j, ks);
-          if (ks == 0) sEa[j] = e;
-        }
-      } else if (tid < 128) {
+      if (tid < 128) {
         const int j = tid >> 2, ks = tid & 3;
         const int e = slice_kstep<1024, 4>(&stV[j * VX_LD], p.conj_b != 0, sBop, j, ks);
         if (ks == 0) sEa[j] = e;
@@ -598,8 +570,6 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
     if (tid == 0) {
       if (p.real_a)
         tc_issue_reala(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
-      else if (p.real_b)
-        tc_issue_realb(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
       else
         tc_issue(tm, tc::smem_u32(sAop), tc::smem_u32(sBop));
       tc::mma_commit(bar);
@@ -655,12 +625,8 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
       const int j = TC_CQ * cqt + q;
       if (p.mode == 0)
         out[((int64_t)blockIdx.y * 32 + j) * p.ldo + c0 + cl] = zdf{accr[q], acci[q]};
-      else if (j0 + j < nj) {
-        if (p.mode == 1)
-          out[c0 + cl + p.ldo * (int64_t)(j0 + j)] = zdf{accr[q], acci[q]};
-        else
-          out[j0 + j + p.ldo * (int64_t)(c0 + cl)] = zdf{accr[q], acci[q]};
-      }
+      else if (j0 + j < nj)
+        out[j0 + j + p.ldo * (int64_t)(c0 + cl)] = zdf{accr[q], acci[q]};
     }
   }
 }
@@ -817,7 +783,7 @@ cudaError_t xhz_tc(EigWork &w, const zdf *X, int64_t ldx, int64_t sX, int nrows,
   p.out = Eb;
   p.ldo = lde;
   p.sO = sE;
-  p.mode = 2;
+  p.mode = 1;
   PP_KT(KT_XHZ, s, (k_longk_tc<<<dim3((nrows + 31) / 32, (w.mcap + 127) / 128, w.B), TC_NT, VX_SMEM, s>>>(
                        p, w.nvec, w.tcErr)));
   count_launch(1);
