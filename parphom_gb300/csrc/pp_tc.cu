@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   for (int p = 0; p < u.nprod; ++p) erow[p] = u.x[p].E[b * u.x[p].sE + (int64_t)rl * u.x[p].es + u.x[p].eo];
   const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + TC_CQ * cqt;
   const uint32_t sa = tc::smem_u32(sAop);
-  int ok = 1;
+  int ok = 1, failed_i = -1;
   for (int i = 0; i < nblk; ++i) {
     const int p = i / ncbw, cb = cb_beg + i % ncbw;
     const uint32_t par3 = (uint32_t)(i & 1);
@@ -293,7 +293,10 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
     // (already complete: makes the copied column exponents visible here)
     done = done && tc::mbar_wait(&bars[1 + (i & 1)], (uint32_t)((i >> 1) & 1));
     ok = __syncthreads_and(done && ok && good);
-    if (!ok) break;
+    if (!ok) {
+      failed_i = i;
+      break;
+    }
     tc::fence_after();
     const int er = erow[p];
     const TcOperand &y = u.y[p];
@@ -337,9 +340,15 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
     tc::fence_after();
   }
   if (!ok) {
-    // let the row-operand copy land before the shared memory is released
+    // let the copies and MMAs still in flight finish (bounded waits) before
+    // the shared and tensor memory are released
     if (tid == 0) {
       tc::mbar_wait(&bars[0], 0, 200000000LL);
+      if (failed_i >= 0) {
+        tc::mbar_wait(&bars[3], (uint32_t)(failed_i & 1), 200000000LL);
+        const int nx = failed_i + 1;
+        if (nx < nblk) tc::mbar_wait(&bars[1 + (nx & 1)], (uint32_t)((nx >> 1) & 1), 200000000LL);
+      }
       atomicExch(&err[b], 1);
     }
     tc::fence_before();
@@ -536,7 +545,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  int ok = 1;
+  int ok = 1, failed_par = -1;
   if (any) load(kc_beg);
   for (int kc = kc_beg; any && kc < kc_end; ++kc) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -577,7 +586,10 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
     if (kc + 1 < kc_end) load(kc + 1);  // in flight while the MMAs run
     const bool done = tc::mbar_wait(bar, (uint32_t)((kc - kc_beg) & 1));
     ok = __syncthreads_and(done && ok);
-    if (!ok) break;
+    if (!ok) {
+      failed_par = (kc - kc_beg) & 1;
+      break;
+    }
     tc::fence_after();
     const int ec = sEc[cl];
 #pragma unroll
@@ -614,7 +626,17 @@ __global__ void __launch_bounds__(TC_NT, 1) k_longk_tc(LongK p, const int *nvec,
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy may land after exit
   if (any) {
-    if (!ok && tid == 0) atomicExch(&err[b], 1);
+    if (!ok) {
+      // the MMAs whose wait gave up may still be running: give them (a
+      // bounded) time to finish before their tensor memory is released
+      if (tid == 0) {
+        atomicExch(&err[b], 1);
+        if (failed_par >= 0) tc::mbar_wait(bar, (uint32_t)failed_par, 200000000LL);
+      }
+      tc::fence_before();
+      __syncthreads();
+      tc::fence_after();
+    }
     if (warp == 0) tc::tmem_dealloc(tm, 512);
   }
   // this thread's row c and its 8 rows j
