@@ -489,7 +489,7 @@ int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_
     cudaGetLastError();
     return run_batch(c, B, o, mcap, want_z);
   }
-  strncpy(c->gkey, key, sizeof(c->gkey) - 1);
+  snprintf(c->gkey, sizeof(c->gkey), "%s", key);
   TRY_CUDA(cudaGraphLaunch(c->gexec, s));
   return PP_OK;
 }
