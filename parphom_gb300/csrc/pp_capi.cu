@@ -636,6 +636,13 @@ int pp_ctx_create(const pp_system *sys, const double *fc, int64_t ldfc, int64_t 
     return code;
   };
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(PP_ERR_CUDA);
+  // the streams of a split batch, created here so that none is created while
+  // a stream capture (the library's or the caller's) is in progress
+  if (cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess) return fail(PP_ERR_CUDA);
+  for (int k = 0; k < pp_ctx::MAX_SPLIT - 1; ++k)
+    if (cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming) != cudaSuccess)
+      return fail(PP_ERR_CUDA);
   cudaStream_t s = c->stream;
   if (cudaMalloc(&g.d_fc, sizeof(double) * n * n) != cudaSuccess) return fail(PP_ERR_NOMEM);
   if (cudaMalloc(&g.d_crys, sizeof(double) * 3 * N) != cudaSuccess) return fail(PP_ERR_NOMEM);
