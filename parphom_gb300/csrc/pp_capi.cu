@@ -457,9 +457,9 @@ bool graphs_enabled() {
 int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   if (!graphs_enabled() || pp::kt_mask) return run_batch(c, B, o, mcap, want_z);
   char key[160];
-  snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d", c->ws, B, o->precision, o->jobz,
+  snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d|%d", c->ws, B, o->precision, o->jobz,
            o->range, o->vel_method, o->vel, (long long)o->il, (long long)o->iu, o->vl, o->vu, o->abstol,
-           want_z ? 1 : 0);
+           want_z ? 1 : 0, split_ways());
   cudaStream_t s = c->stream;
   if (c->gexec && strcmp(key, c->gkey) == 0) {
     TRY_CUDA(cudaGraphLaunch(c->gexec, s));
