@@ -42,17 +42,21 @@ def rounds(nq: int, world: int, batch: int) -> int:
     return math.ceil(math.ceil(nq / world) / batch) if nq > 0 else 0
 
 
-def init_group(world: int, rank: int):
+def init_group(world: int, rank: int, timeout_s: float = 600.0):
     """The gloo process group used for the result gathering (created on the
-    default group when torch.distributed is not initialised yet)."""
+    default group when torch.distributed is not initialised yet).  A rank that
+    dies or never reaches a gathering makes the others' next collective fail
+    with an error after at most timeout_s seconds instead of waiting forever."""
+    import datetime
     import torch.distributed as dist
     if world == 1:
         return None
+    timeout = datetime.timedelta(seconds=timeout_s)
     if not dist.is_initialized():
-        dist.init_process_group("gloo", rank=rank, world_size=world)
+        dist.init_process_group("gloo", rank=rank, world_size=world, timeout=timeout)
     if dist.get_backend() == "gloo":
         return None  # the default group already is gloo
-    return dist.new_group(backend="gloo")
+    return dist.new_group(backend="gloo", timeout=timeout)
 
 
 def max_over_ranks(x: float, world: int, group=None) -> float:

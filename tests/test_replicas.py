@@ -59,6 +59,43 @@ def test_two_ranks_gloo(tmp_path, nq, batch):
     assert r0[1] == r1[1] == 2.0                                      # max over ranks
 
 
+def _worker_dies(rank, world, port, out_dir):
+    import time
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    group = replicas.init_group(world, rank, timeout_s=20.0)
+    q = np.zeros((6, 3))
+
+    def solve(qb):
+        if rank == 1:
+            os._exit(3)   # a rank that dies between two gatherings
+        return [0.0] * len(qb)
+
+    t0 = time.time()
+    try:
+        replicas.run_sharded(q, 1, solve, (lambda t, r: None) if rank == 0 else None, world, rank, group)
+        status = "finished"
+    except Exception as e:   # the surviving rank learns of it from its collective
+        status = type(e).__name__
+    with open(os.path.join(out_dir, f"status{rank}.txt"), "w") as f:
+        f.write(f"{status} {time.time() - t0:.1f}")
+
+
+def test_dead_rank_fails_the_gathering(tmp_path):
+    import torch.multiprocessing as mp
+
+    ctx = mp.start_processes(_worker_dies, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=False,
+                             start_method="spawn")
+    for p in ctx.processes:
+        p.join(120)
+        if p.is_alive():   # our own child, by its handle
+            p.kill()
+    status, dt = (tmp_path / "status0.txt").read_text().split()
+    assert status != "finished"
+    assert float(dt) < 60.0
+    assert not (tmp_path / "status1.txt").exists()
+
+
 def test_one_rank_writes_in_order():
     q = np.random.default_rng(0).standard_normal((11, 3))
     out = []
