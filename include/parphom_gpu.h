@@ -52,6 +52,9 @@ typedef struct pp_ctx pp_ctx;
 #define PP_INFO_NOMEM 4       /* workspace too small for all eigenvectors      */
 #define PP_INFO_NOTCOMP 8     /* an eigenvalue was not computed                */
 #define PP_INFO_TIMEOUT 16    /* a bounded device wait gave up: results invalid */
+#define PP_INFO_NAN 32        /* non-finite input found on the device (entry
+                                 points whose input is device memory only):
+                                 no eigenvalues returned                      */
 
 /* Precision forms. */
 #define PP_PREC_FP64 0        /* plain IEEE double throughout                  */
@@ -204,12 +207,15 @@ PP_API int64_t pp_kernel_launches(void);
 
 /* Eigenvalues of one Hermitian matrix with no device allocation at all.
  * No counterpart in the reference: it exists for callers that cannot
- * allocate device memory (inside a stream capture or a pipeline they do not
- * own, drivers that hand over a fixed device pool).  The FP64 reduction and
- * bisection use one fixed scratch array of about 1.5 MB compiled into the
- * library, which every GPU that loads the library keeps until exit.
+ * allocate device memory — drivers that hand over a fixed device pool and
+ * forbid hidden allocations, stream-ordered pipelines the caller does not
+ * own (where an allocation would synchronise the device), and long runs that
+ * must not grow the device footprint.  The FP64 reduction and bisection use
+ * one fixed scratch array of about 2.0 MB compiled into the library, which
+ * every GPU that loads the library keeps until exit.
  *   a_dev   n x n complex FP64 column-major device matrix, ld lda; only the
  *           upper triangle is read (as pzheevx with uplo 'U'); overwritten.
+ *           A non-finite element gives info PP_INFO_NAN and m = 0.
  *   n       1 <= n <= PP_NOALLOC_MAX_N, else PP_ERR_SIZE; lda <= 1536 too.
  *   range   'A', 'I' (il..iu, 1-based) or 'V' (eigenvalues in (vl, vu],
  *           bounds in the matrix's own units), abstol as in pzheevx.
@@ -217,10 +223,12 @@ PP_API int64_t pp_kernel_launches(void);
  *           one int64 each (info: pzheevx-style bits); all device memory.
  * Enqueued on `stream`.  The first call on a device resolves the array's
  * address (cudaGetSymbolAddress) with that device current: make that first
- * call before any stream capture.  All calls share the one array and leave
- * their contents in it; calls that overlap on the GPU (different streams,
- * threads or captured graphs running at once) race on it.  Do not enable
- * pp_ktimer_enable around it (the timer creates CUDA events). */
+ * call before any stream capture, and do not use the entry point across a
+ * cudaDeviceReset (the address is kept for the life of the process).  All
+ * calls share the one array and leave their contents in it (each call resets
+ * what must start at zero); calls that overlap on the GPU (different streams
+ * or threads running at once) race on it.  Do not enable pp_ktimer_enable
+ * around it (the timer creates CUDA events). */
 PP_API int pp_heevx_values_noalloc(double *a_dev, int64_t lda, int64_t n, char range, double vl, double vu,
                                    int64_t il, int64_t iu, double abstol, double *w_dev, int64_t *m_dev,
                                    int64_t *info_dev, void *stream);

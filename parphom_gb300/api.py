@@ -28,6 +28,8 @@ INFO_NOCONV = 1
 INFO_NOORTH = 2
 INFO_NOMEM = 4
 INFO_NOTCOMP = 8
+INFO_TIMEOUT = 16
+INFO_NAN = 32
 
 EXPORTED = ("pp_ctx_create", "pp_ctx_destroy", "pp_solve_batch", "pp_solve_batch_device", "pp_dynamical_matrix",
             "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report",

@@ -18,6 +18,32 @@ namespace pp {
 static std::atomic<int64_t> g_launches{0};
 void count_launch(int64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
+int device_index() {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return (dev >= 0 && dev < PP_MAX_DEVICES) ? dev : -1;
+}
+
+int device_sms() {
+  static std::mutex mu;
+  static int sms[PP_MAX_DEVICES] = {};
+  const int dev = device_index();
+  if (dev < 0) return 1;
+  std::lock_guard<std::mutex> g(mu);
+  if (!sms[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    sms[dev] = v > 0 ? v : 1;
+  }
+  return sms[dev];
+}
+
 unsigned kt_mask = 0;
 static const char *kt_names[KT_N] = {"assemble", "colupd", "refl", "hemv", "dots", "wcorr", "wfin", "her2k",
                                      "bisect", "invit", "vhx", "btred", "applyV", "vel", "xhz"};

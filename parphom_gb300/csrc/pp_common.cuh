@@ -183,3 +183,4 @@ PP_HD z64 zconj(z64 a) { return z64{a.re, -a.im}; }
 #define PP_INFO_NOMEM 4
 #define PP_INFO_NOTCOMP 8
 #define PP_INFO_TIMEOUT 16
+#define PP_INFO_NAN 32

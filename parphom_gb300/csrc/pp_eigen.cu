@@ -25,6 +25,7 @@
 // form) or df (double-float on the FP32 pipes, the mixed form).
 #include <atomic>
 #include <algorithm>
+#include <mutex>
 #include <cfloat>
 #include <type_traits>
 #include <cstdio>
@@ -532,17 +533,8 @@ __global__ void __launch_bounds__(256) k_her2k(C<R> *Ab, int64_t lda, int64_t sA
     }
 }
 
-// Persistent hemv blocks: HL_BPS per SM.
-static int hemv_blocks() {
-  static int v = 0;
-  if (!v) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    v = std::max(1, sms) * HL_BPS;
-  }
-  return v;
-}
+// Persistent hemv blocks: HL_BPS per SM of the current device.
+static int hemv_blocks() { return device_sms() * HL_BPS; }
 
 template <class R>
 cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
@@ -848,16 +840,18 @@ size_t bisect_smem(int64_t n, int mixed) {
   return b <= 200 * 1024 ? b : 0;
 }
 
+// The attribute applies to the current device only: a high-water mark is
+// kept per device.
 cudaError_t prepare_bisect(size_t bytes) {
-  static std::atomic<int> done{0};
+  static std::mutex mu;
+  static int done[PP_MAX_DEVICES] = {};
   const int need = (int)bytes;
-  if (need <= done.load() || need > 200 * 1024) return cudaSuccess;
+  if (need > 200 * 1024) return cudaSuccess;
+  const int dev = device_index();
+  std::lock_guard<std::mutex> g(mu);
+  if (dev >= 0 && need <= done[dev]) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
-  if (e == cudaSuccess) {
-    int cur = done.load();
-    while (need > cur && !done.compare_exchange_weak(cur, need)) {
-    }
-  }
+  if (e == cudaSuccess && dev >= 0) done[dev] = need;
   return e;
 }
 

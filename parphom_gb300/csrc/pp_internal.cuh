@@ -12,6 +12,14 @@ namespace pp {
 // Counts kernel launches made by this library (pp_kernel_launches()).
 void count_launch(int64_t k = 1);
 
+// Kernel attributes (cudaFuncSetAttribute) and device properties apply to
+// one device: caches of them are kept per device index, 0 .. PP_MAX_DEVICES-1.
+constexpr int PP_MAX_DEVICES = 64;
+// The current device's index, or -1 if it cannot be read or is out of range.
+int device_index();
+// Number of SMs of the current device (cached per device; 1 if unknown).
+int device_sms();
+
 // Optional per-launch CUDA-event timing of selected kernel classes
 // (pp_ktimer_enable / pp_ktimer_report).
 enum KClass {

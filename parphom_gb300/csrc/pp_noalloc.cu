@@ -1,14 +1,15 @@
 // Hermitian eigenvalues without any device allocation.
 //
-// Some callers cannot call cudaMalloc: code that runs inside a CUDA-graph
-// capture or a stream-ordered pipeline they do not own, Fortran drivers that
-// hand the library a pre-sized device pool and forbid hidden allocations,
-// and callers that must not grow the device footprint once a run has
-// started.  pp_heevx_values_noalloc serves them: the caller passes the
-// matrix and the output buffers, and every scratch buffer of the FP64
-// reduction-and-bisection pipeline lives in the file-scope device array
-// below, of fixed size, which every GPU that loads the library holds until
-// the process exits.
+// Some callers cannot call cudaMalloc: drivers that hand the library a
+// pre-sized device pool and forbid hidden allocations (an allocation there
+// would break the pool's accounting or fail outright once the pool owns the
+// memory), stream-ordered pipelines they do not own, where an allocation
+// would synchronise the device, and long runs that must not grow the device
+// footprint once started.  pp_heevx_values_noalloc serves them: the caller
+// passes the matrix and the output buffers, and every scratch buffer of the
+// FP64 reduction-and-bisection pipeline lives in the file-scope device array
+// below, of fixed size (about 2.0 MB for n <= 1536), which every GPU that
+// loads the library holds until the process exits.
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -40,11 +41,14 @@ constexpr size_t OFF_WW = al(OFF_SCAL + 16 * 4);
 constexpr size_t OFF_RNG = al(OFF_WW + 8 * (size_t)NOALLOC_MAX_N);
 constexpr size_t OFF_TINFO = al(OFF_RNG + 8 * 8);
 constexpr size_t OFF_INFO = al(OFF_TINFO + 8 * 8);
-constexpr size_t SCRATCH_BYTES = al(OFF_INFO + 8);
+constexpr size_t OFF_BAD = al(OFF_INFO + 8);
+constexpr size_t SCRATCH_BYTES = al(OFF_BAD + 8);
+// The W panel (0.79 MB) and the mat-vec partial sums (1.18 MB) dominate.
+static_assert(SCRATCH_BYTES > 1900000 && SCRATCH_BYTES < 2100000, "scratch size as documented: about 2.0 MB");
 
 }  // namespace
 
-// The scratch array (about 1.5 MB).  Device code could name it directly;
+// The scratch array (about 2.0 MB).  Device code could name it directly;
 // host code only ever uses the address cudaGetSymbolAddress returns for the
 // current device, never the host-side symbol itself.
 static __device__ __align__(256) unsigned char pp_noalloc_scratch[SCRATCH_BYTES];
@@ -56,6 +60,9 @@ std::mutex g_mu;
 void *g_scratch[MAX_DEVICES] = {};
 
 // Once per device, with that device current: resolve the array's address.
+// The address is kept for the life of the process: after a cudaDeviceReset
+// the module is loaded again and the array may move, so the entry point must
+// not be used across a device reset.
 int scratch_for_current_device(unsigned char **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -77,24 +84,39 @@ int scratch_for_current_device(unsigned char **out) {
   return PP_OK;
 }
 
-// Lower triangle := conjugate of the upper triangle (only 'U' is referenced,
-// as pzheevx does); also zero the per-call state that must start at zero.
-__global__ void k_na_prepare(z64 *A, int64_t lda, int64_t n, int *nvec, int64_t *info) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t c = blockIdx.y;
-  if (r == 0 && c == 0) {
+// Zero the per-call state that must start at zero (the array keeps what the
+// previous call left in it).
+__global__ void k_na_reset(int *nvec, int64_t n, int64_t *info, int *bad) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
     *nvec = (int)n;
     *info = 0;
+    *bad = 0;
   }
-  if (r >= n || c >= n || r <= c) return;
-  const z64 u = A[c + lda * r];
-  A[r + lda * c] = z64{u.re, -u.im};
 }
 
-__global__ void k_na_finish(const int64_t *rng, const int64_t *info_in, int64_t *m_out, int64_t *info_out) {
+// Lower triangle := conjugate of the upper triangle (only 'U' is referenced,
+// as pzheevx does).  A non-finite element of the upper triangle is replaced
+// by zero and flagged: the call then reports PP_INFO_NAN and no eigenvalues
+// (pp_solve_batch rejects such input on the host; here the matrix is only
+// in device memory).
+__global__ void k_na_prepare(z64 *A, int64_t lda, int64_t n, int *bad) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  if (r >= n || c >= n || r < c) return;
+  z64 u = A[c + lda * r];
+  if (!isfinite(u.re) || !isfinite(u.im)) {
+    u = z64{0.0, 0.0};
+    A[c + lda * r] = u;
+    atomicExch(bad, 1);
+  }
+  if (r > c) A[r + lda * c] = z64{u.re, -u.im};
+}
+
+__global__ void k_na_finish(const int64_t *rng, const int64_t *info_in, const int *bad, int64_t *m_out,
+                            int64_t *info_out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    *m_out = rng[2];
-    *info_out = *info_in;
+    *m_out = *bad ? 0 : rng[2];
+    *info_out = *info_in | (*bad ? PP_INFO_NAN : 0);
   }
 }
 
@@ -141,16 +163,17 @@ extern "C" PP_API int pp_heevx_values_noalloc(double *a_dev, int64_t lda, int64_
   w.rng = (int64_t *)(base + OFF_RNG);
   w.tinfo = (double *)(base + OFF_TINFO);
   w.info = (int64_t *)(base + OFF_INFO);
-  k_na_prepare<<<dim3((unsigned)((n + 127) / 128), (unsigned)n), 128, 0, s>>>((z64 *)a_dev, lda, n, w.nvec,
-                                                                               w.info);
+  int *bad = (int *)(base + OFF_BAD);
+  k_na_reset<<<1, 32, 0, s>>>(w.nvec, n, w.info, bad);
+  k_na_prepare<<<dim3((unsigned)((n + 127) / 128), (unsigned)n), 128, 0, s>>>((z64 *)a_dev, lda, n, bad);
   cudaError_t e = pp::tridiagonalize<double>(w, s);
   if (e == cudaSuccess) e = pp::tridiag_eigenvalues(w, range, vl, vu, il, iu, abstol, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(w_dev, w.w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) {
-    k_na_finish<<<1, 32, 0, s>>>(w.rng, w.info, m_dev, info_dev);
+    k_na_finish<<<1, 32, 0, s>>>(w.rng, w.info, bad, m_dev, info_dev);
     e = cudaGetLastError();
   }
-  pp::count_launch(2);
+  pp::count_launch(3);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return PP_ERR_CUDA;

@@ -30,6 +30,7 @@
 #include <cfloat>
 #include <cstdint>
 #include <cstdlib>
+#include <mutex>
 #include <cuda_bf16.h>
 
 #include "pp_internal.cuh"
@@ -669,12 +670,17 @@ bool tc_enabled() {
 size_t her2k_tc_bytes(int64_t nmax) { return (size_t)((nmax + 127) / 128) * TC_RBLK; }
 int64_t her2k_tc_exps(int64_t nmax) { return 2 * ((nmax + 127) / 128) * 128; }
 
+// Opt the tensor-core kernels into their shared memory on the current device
+// (the attribute is per device; done once per device, outside any capture).
 cudaError_t prepare_her2k_tc() {
-  static int done = 0;
-  if (done) return cudaSuccess;
+  static std::mutex mu;
+  static bool done[PP_MAX_DEVICES] = {};
+  const int dev = device_index();
+  std::lock_guard<std::mutex> g(mu);
+  if (dev >= 0 && done[dev]) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(k_cupd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_longk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, VX_SMEM);
-  if (e == cudaSuccess) done = 1;
+  if (e == cudaSuccess && dev >= 0) done[dev] = true;
   return e;
 }
 

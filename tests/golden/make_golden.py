@@ -1,8 +1,8 @@
 """Generate the committed golden fixtures from the reference's example data.
 
-Run in a checkout that has the reference at REF (default /root/reference):
+Run with the root of a qtm-iisc/PARPHOM checkout as the one required argument:
 
-    python tests/golden/make_golden.py [REF]
+    python tests/golden/make_golden.py REF
 
 Inputs (all from qtm-iisc/PARPHOM):
   Force_Constant_Generation/Examples/tblg_21.8/FORCE_CONSTANTS  (HDF5, (28,28,3,3) f64)
@@ -18,6 +18,9 @@ Outputs:
                                      produced from the shipped FORCE_CONSTANTS
   tests/golden/tblg21_8_oracle.npz   oracle outputs (w_cm, velocities) at the
                                      K-equivalent points and Gamma
+  tests/golden/inputs/*              the example input files (inp*.dat, inp.dos*)
+                                     of Phonon_Calculations/Examples, copied
+                                     unchanged, for the input-parser tests
 """
 from __future__ import annotations
 
@@ -48,7 +51,23 @@ def parse_h5dump_eigs(path):
     return out
 
 
-def main(ref="/root/reference"):
+# example input files copied for the parser tests: (example dir, file name)
+EXAMPLE_INPUTS = [("tblg_21.8", "inp.dat"), ("tblg_21.8", "inp.dos"), ("tblg_21.8", "inp.dos_tersoff"),
+                  ("tblg_21.8", "inp_symm.dat"), ("tbmos2_38.2", "inp.dat"), ("tbmos2_38.2", "inp_dos.dat"),
+                  ("tbwse2_21.8", "inp.dat"), ("tbwse2_21.8", "inp.dos")]
+
+
+def copy_example_inputs(ref):
+    out = os.path.join(HERE, "inputs")
+    os.makedirs(out, exist_ok=True)
+    for d, f in EXAMPLE_INPUTS:
+        src = os.path.join(ref, "Phonon_Calculations/Examples", d, f)
+        with open(src, "rb") as fi, open(os.path.join(out, f"{d}__{f}"), "wb") as fo:
+            fo.write(fi.read())
+
+
+def main(ref):
+    copy_example_inputs(ref)
     ex = os.path.join(ref, "Phonon_Calculations/Examples/tblg_21.8")
     fcf = os.path.join(ref, "Force_Constant_Generation/Examples/tblg_21.8/FORCE_CONSTANTS")
     dset = h5.read_dataset(fcf, "force_constants")
@@ -77,4 +96,6 @@ def main(ref="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <root of a qtm-iisc/PARPHOM checkout>")
+    main(sys.argv[1])

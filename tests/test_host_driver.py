@@ -106,3 +106,55 @@ def test_bad_inputs_fail_with_a_message(exe, tmp_path):
     assert r.returncode == 1 and "Invalid input for eigenvalue indices" in r.stderr
     r = subprocess.run([exe, "--h5-read", str(tmp_path / "inp.dat"), "x"], capture_output=True, text=True)
     assert r.returncode == 1 and "not an HDF5 file" in r.stderr
+
+
+# The reference's own example input files (copied unchanged by
+# tests/golden/make_golden.py).  Expected fields are read off each file by
+# the rules of read_input.F90: comments cut at '!' or '#' (:95-103), keys
+# upper-cased with spaces or underscores (:110-245), a trailing '/' added to
+# locations (:415-440), range 'A' sets il=1, iu=natom, vl=vu=0 (:457-470),
+# group velocity forces comp_evec 'V' (:483-485), '.hdf5' appended to the
+# output name (:487-513).
+_TBLG = "../../../Force_Constant_Generation/Examples/tblg_21.8/"
+_EXPECT = {
+    "tblg_21.8__inp.dat": dict(natom=28, atom_types=1, atom_style="molecular", q_name="q_points_band.dat",
+                               nqpt=300, fc_location=_TBLG, fc_name="FORCE_CONSTANTS", compute_eigvecs=True,
+                               comp_evec="V", group_velocity=True, velocity_method="A", range_="A", il=1, iu=28,
+                               vl=0.0, vu=0.0, mb=4, nb=4, abstol=1e-14, orfac=1e-14,
+                               output_name="phbands_21.8.hdf5", output_location="./", print_progress=True),
+    "tblg_21.8__inp.dos": dict(nqpt=27, q_name="dos_21.8_15X15.dat", compute_eigvecs=False, comp_evec="N",
+                               group_velocity=False, velocity_method="A", mb=8, nb=8, abstol=1e-16,
+                               output_name="phbands_21.8_dos_15X15.hdf5", output_location="./"),
+    "tblg_21.8__inp.dos_tersoff": dict(lammps_location=_TBLG, lammps_name="lammps.dat_tersoff",
+                                       fc_name="FORCE_CONSTANTS_TERSOFF", output_location="./",
+                                       output_name="phbands_21.8_dos_15X15_tersoff.hdf5"),
+    "tblg_21.8__inp_symm.dat": dict(q_name="q_pt_symm.dat", nqpt=3, velocity_method="C", group_velocity=True,
+                                    comp_evec="V", output_name="phbandsymm.hdf5"),
+    "tbmos2_38.2__inp.dat": dict(natom=42, atom_types=6, atom_style="atomic",
+                                 lammps_location="/home/mshinjan/Phonons/MoirePhonons/Force_Constant_Generation/"
+                                                 "Examples/tbmos2_38.2/",
+                                 q_name="qpt_bands_KKp.dat", nqpt=201, mb=16, nb=16, iu=42, velocity_method="A",
+                                 group_velocity=True),
+    "tbmos2_38.2__inp_dos.dat": dict(nqpt=1802, fc_location="./", fc_name="FC_hdf5", group_velocity=False,
+                                     compute_eigvecs=True, comp_evec="V", mb=32, nb=32,
+                                     output_name="phdos_9.43_mos2.hdf5"),
+    "tbwse2_21.8__inp.dat": dict(q_name="q_points_band.dat", nqpt=300, lammps_name="lammps.dat_final",
+                                 fc_location="../../../Force_Constant_Generation/Examples/tbwse2_21.8/",
+                                 velocity_method="A", group_velocity=True),
+    "tbwse2_21.8__inp.dos": dict(q_name="full_grid_100X100", nqpt=10000, abstol=1e-15, orfac=1e-15,
+                                 fc_location="/home/mshinjan/Twister/examples/Homobilayer_hex/WSe2/Angle_21.78/"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(_EXPECT))
+def test_reference_example_inputs(exe, golden_dir, tmp_path, name):
+    """Both parsers (C++ host driver and its Python mirror) read each shipped
+    example input to the values the reference's parser gives."""
+    src = os.path.join(golden_dir, "inputs", name)
+    dst = tmp_path / "inp.dat"
+    dst.write_bytes(open(src, "rb").read())
+    c = json.loads(run(exe, "--parse-input", str(dst), cwd=tmp_path))
+    p = dataclasses.asdict(inputs.read_input(str(dst)))
+    assert c == p
+    for k, v in _EXPECT[name].items():
+        assert p[k] == v, (name, k, p[k], v)
