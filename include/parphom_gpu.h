@@ -96,7 +96,10 @@ typedef struct pp_eig_opts {
   double orfac;       /* accepted for interface parity; clusters are formed by
                          the library's own relative-gap rule                    */
   int32_t raw_lambda; /* nonzero: w holds eigenvalues of D instead of cm^-1    */
-  int32_t want_resid; /* nonzero: fill resid[] with ||D z - lambda z||_2        */
+  int32_t want_resid; /* nonzero: per-eigenpair error estimates in FP64 into
+                         resid[], werr[], zerr[] of the result view (needs the
+                         full eigenvectors: computed internally if not asked
+                         for; costs an FP64 product D Z per q-point)         */
 } pp_eig_opts;
 
 /* Output buffers for nq q-points (host or device memory depending on call).
@@ -104,7 +107,17 @@ typedef struct pp_eig_opts {
  *   w[j + ldw*t]                      frequency in cm^-1 (or lambda)
  *   z[2*(r + ldz*j) + zstride*t]      (re, im) of eigenvector j, row r
  *   vel[d + 3*j + velstride*t]        group velocity, direction d, m/s
- *   resid[j + ldw*t]                  residual norm (if want_resid)          */
+ * With want_resid (each may be NULL), computed in FP64 against D(q)
+ * assembled in FP64, for the normalised eigenpair (lambda_j, z_j):
+ *   resid[j + ldw*t]  ||D z - lambda z||_2 (units of D)
+ *   werr[j + ldw*t]   estimated bound on the error of w[j] (cm^-1, or lambda
+ *                     units with raw_lambda): min(resid, |lambda - rho| +
+ *                     ||D z - rho z||^2 / gap), rho the Rayleigh quotient,
+ *                     gap the distance to the nearest other computed
+ *                     eigenvalue, carried through sign(l) sqrt|l|
+ *   zerr[j + ldw*t]   estimated bound on sin(angle) between z_j and the exact
+ *                     eigenvector: min(1, ||D z - rho z|| / gap) (large inside
+ *                     clusters of near-degenerate modes)                    */
 typedef struct pp_result_view {
   int64_t *m;         /* [nq] number of eigenvalues found (comp_num_eval)     */
   int64_t *nz;        /* [nq] number of eigenvectors (comp_num_evec)          */
@@ -116,6 +129,8 @@ typedef struct pp_result_view {
   double *vel;        /* may be NULL                                          */
   int64_t velstride;  /* in doubles                                           */
   double *resid;      /* may be NULL                                          */
+  double *werr;       /* may be NULL                                          */
+  double *zerr;       /* may be NULL                                          */
 } pp_result_view;
 
 /* Create a context on the current CUDA device: uploads Phi (after the
@@ -125,6 +140,15 @@ typedef struct pp_result_view {
  * Replaces: the state set up by read_lammps_data / read_force_constants
  * (main.F90:53-62) as seen by create_dynamical_matrix. */
 PP_API int pp_ctx_create(const pp_system *sys, const double *fc, int64_t ldfc, int64_t flags, pp_ctx **out);
+
+/* Replace the force constants of a context, keeping its geometry tables:
+ * Phi is copied (host memory, or device memory with fc_on_device = 1: e.g.
+ * a torch tensor of the differentiation layer, column-major with ld ldfc,
+ * upper triangle referenced), symmetrised as at creation and the boundary
+ * block tables rebuilt from its non-zero blocks.  Synchronous.  No
+ * counterpart in the reference (one Phi per run); used when fitting force
+ * constants, where Phi changes between forward passes. */
+PP_API int pp_ctx_update_fc(pp_ctx *ctx, const double *fc, int64_t ldfc, int64_t flags, int32_t fc_on_device);
 
 /* Free every device resource of the context. */
 PP_API int pp_ctx_destroy(pp_ctx *ctx);
@@ -169,6 +193,33 @@ PP_API int pp_dos_triangulation(const double *freq, int64_t ldf, int64_t nk, int
 PP_API int pp_dos_smearing(int32_t method, const double *freq, int64_t ldf, int64_t nq, int64_t nbands,
                            const double *weights, double width, const double *energy, int64_t ne, int64_t natom,
                            double *dos);
+
+/* Device-resident forms of the two DOS entry points, fed straight from the
+ * outputs of pp_solve_batch_device (no host round trip, no HDF5 file):
+ * freq_dev is its w output (freq_dev[q*ldf + b], ldf = its ldw), func_dev an
+ * optional per-(q, band) weight with its own leading dimension ldfunc (e.g.
+ * from pp_velocity_weights_device: the transport DOS), tri_dev, energy_dev,
+ * weights_dev and the outputs (ne doubles each) all device memory.  Results
+ * as pp_dos_triangulation / pp_dos_smearing; the bands are summed in a
+ * different order (last-bit differences).  Enqueued on `stream`; nothing is
+ * allocated.  Replaces the same routines as the host forms
+ * (bz_integration.f90:12-199 as called from pyphutil.py:214-359). */
+PP_API int pp_dos_triangulation_device(const double *freq_dev, int64_t ldf, int64_t nk, int64_t nbands,
+                                       const double *func_dev, int64_t ldfunc, const int64_t *tri_dev, int64_t ntri,
+                                       const double *energy_dev, int64_t ne, double *dos_dev, double *nd_dev,
+                                       void *stream);
+PP_API int pp_dos_smearing_device(int32_t method, const double *freq_dev, int64_t ldf, int64_t nq, int64_t nbands,
+                                  const double *weights_dev, double width, const double *energy_dev, int64_t ne,
+                                  int64_t natom, double *dos_dev, void *stream);
+
+/* Weights of a velocity-weighted (transport) DOS from the velocity output
+ * of pp_solve_batch_device (vel_dev[q*velstride + 3*j + d], m/s):
+ * func_dev[q*ldfunc + j] = v_a v_b of mode j (a, b in 0..2: x, y, z), or
+ * |v|^2 with a = b = -1.  The func argument of pyphutil's
+ * density_of_states (pyphutil.py:214-260), built on the device.  Enqueued on
+ * `stream`. */
+PP_API int pp_velocity_weights_device(const double *vel_dev, int64_t velstride, int64_t nq, int64_t nbands, int32_t a,
+                                      int32_t b, double *func_dev, int64_t ldfunc, void *stream);
 
 /* D(q) (derivative = 0) or dD/dq_k (derivative = k in 1..3, vel_method 'A'
  * or 'C') for one q, written as the full Hermitian matrix (upper triangle
@@ -239,6 +290,17 @@ PP_API int pp_heevx_values_noalloc(double *a_dev, int64_t lda, int64_t n, char r
  * "<class> <launches> <total milliseconds>". */
 PP_API int pp_ktimer_enable(const char *names);
 PP_API int pp_ktimer_report(char *buf, int64_t len);
+
+/* Test hook for the bounded device waits (no counterpart in the reference).
+ * Arms a one-shot stall: the next mixed-form tensor-core trailing update
+ * whose batch contains batch matrix `matrix` (0-based index within one
+ * pp_solve_batch batch) waits, before its first copy wait, on a barrier that
+ * nothing completes, for at most `cycles` SM clocks (0 .. 2e9), then takes
+ * the time-out path: it waits (bounded) for its own copies in flight, frees
+ * its tensor memory and returns; later launches skip that matrix and its
+ * info gets PP_INFO_TIMEOUT.  matrix = -1 disarms.  The call that consumes
+ * the stall runs without the captured graph. */
+PP_API int pp_debug_stall_tc_wait(int64_t matrix, int64_t cycles);
 
 #ifdef __cplusplus
 }

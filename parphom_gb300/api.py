@@ -33,7 +33,9 @@ INFO_NAN = 32
 
 EXPORTED = ("pp_ctx_create", "pp_ctx_destroy", "pp_solve_batch", "pp_solve_batch_device", "pp_dynamical_matrix",
             "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report",
-            "pp_heevx_values_noalloc", "pp_backward_phi", "pp_solve_multi")
+            "pp_heevx_values_noalloc", "pp_backward_phi", "pp_solve_multi", "pp_debug_stall_tc_wait",
+            "pp_ctx_update_fc", "pp_dos_triangulation_device", "pp_dos_smearing_device",
+            "pp_velocity_weights_device")
 PP_ERR_SIZE = 1008
 PP_NOALLOC_MAX_N = 1536
 
@@ -57,7 +59,7 @@ class PPEigOpts(ctypes.Structure):
 
 class PPResultView(ctypes.Structure):
     _fields_ = [("m", _ip), ("nz", _ip), ("w", _dp), ("ldw", _i64), ("z", _dp), ("ldz", _i64), ("zstride", _i64),
-                ("vel", _dp), ("velstride", _i64), ("resid", _dp)]
+                ("vel", _dp), ("velstride", _i64), ("resid", _dp), ("werr", _dp), ("zerr", _dp)]
 
 
 class PPError(RuntimeError):
@@ -86,6 +88,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L = ctypes.CDLL(path)
     L.pp_ctx_create.argtypes = [ctypes.POINTER(PPSystem), _dp, _i64, _i64, ctypes.POINTER(ctypes.c_void_p)]
     L.pp_ctx_create.restype = ctypes.c_int
+    L.pp_ctx_update_fc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _i64, _i64, ctypes.c_int32]
+    L.pp_ctx_update_fc.restype = ctypes.c_int
     L.pp_ctx_destroy.argtypes = [ctypes.c_void_p]
     L.pp_ctx_destroy.restype = ctypes.c_int
     L.pp_solve_batch.argtypes = [ctypes.c_void_p, _dp, _i64, _i64, ctypes.POINTER(PPEigOpts),
@@ -110,6 +114,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.pp_backward_phi.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _i64, ctypes.c_void_p, _i64, _i64, _i64,
                                   ctypes.c_void_p, _i64, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
     L.pp_backward_phi.restype = ctypes.c_int
+    L.pp_debug_stall_tc_wait.argtypes = [_i64, _i64]
+    L.pp_debug_stall_tc_wait.restype = ctypes.c_int
     L.pp_ktimer_enable.argtypes = [ctypes.c_char_p]
     L.pp_ktimer_enable.restype = ctypes.c_int
     L.pp_ktimer_report.argtypes = [ctypes.c_char_p, _i64]
@@ -144,11 +150,13 @@ class EigOpts:
     vel_method: str = "A"
     precision: int = PP_PREC_FP64
     raw_lambda: bool = False
+    want_resid: bool = False   # per-eigenpair error estimates (Result.resid/werr/zerr)
 
     def to_c(self) -> PPEigOpts:
         return PPEigOpts(self.jobz.encode()[:1], self.range.encode()[:1], self.vel_method.encode()[:1], b"U",
                          int(bool(self.vel)), int(self.precision), float(self.vl), float(self.vu), int(self.il),
-                         int(self.iu), float(self.abstol), float(self.orfac), int(bool(self.raw_lambda)), 0)
+                         int(self.iu), float(self.abstol), float(self.orfac), int(bool(self.raw_lambda)),
+                         int(bool(self.want_resid)))
 
 
 @dataclasses.dataclass
@@ -159,6 +167,9 @@ class Result:
     z: Optional[np.ndarray]    # (nq, n, mz) complex, column j = eigenvector j; mz = n, or iu-il+1 for range I
     vel: Optional[np.ndarray]  # (nq, n, 3) m/s
     info: np.ndarray       # (nq,) pzheevx-style bits
+    resid: Optional[np.ndarray] = None  # (nq, n) ||D z - lambda z|| (want_resid)
+    werr: Optional[np.ndarray] = None   # (nq, n) error bound of w (cm^-1, or lambda units)
+    zerr: Optional[np.ndarray] = None   # (nq, n) bound on sin(angle) of each eigenvector
 
 
 class PhononContext:
@@ -191,6 +202,21 @@ class PhononContext:
         if crys is None:
             crys = crys_from_positions(cell.lat, cell.real_pos)
         return cls(cell.lat, crys, cell.real_pos, cell.masses, cell.at_types, fc, **kw)
+
+    def update_fc(self, fc, enforce_asr: bool = False) -> None:
+        """Replace Phi (host array, symmetric (3N, 3N)); geometry tables kept."""
+        fcf = np.asfortranarray(fc, np.float64)
+        rc = self._lib.pp_ctx_update_fc(self._h, ctypes.c_void_p(fcf.ctypes.data), self.n,
+                                        PP_FLAG_ENFORCE_ASR if enforce_asr else 0, 0)
+        if rc != 0:
+            raise PPError(rc, "pp_ctx_update_fc")
+
+    def update_fc_device(self, fc_ptr: int, ldfc: int, enforce_asr: bool = False) -> None:
+        """Replace Phi from device memory (column-major float64, ld ldfc)."""
+        rc = self._lib.pp_ctx_update_fc(self._h, ctypes.c_void_p(int(fc_ptr)), int(ldfc),
+                                        PP_FLAG_ENFORCE_ASR if enforce_asr else 0, 1)
+        if rc != 0:
+            raise PPError(rc, "pp_ctx_update_fc")
 
     def close(self):
         if getattr(self, "_h", None):
@@ -236,9 +262,11 @@ class PhononContext:
         z = np.zeros((nq, mz, n), np.complex128) if (vecs and want_z) else None
         vel = np.zeros((nq, n, 3)) if opts.vel else None
         zv = z.view(np.float64) if z is not None else None
+        errs = [np.zeros((nq, n)) for _ in range(3)] if opts.want_resid else [None] * 3
         rv = PPResultView(m.ctypes.data_as(_ip), nz.ctypes.data_as(_ip), _p(w), n,
                           _p(zv) if zv is not None else None, n, 2 * n * mz,
-                          _p(vel) if vel is not None else None, 3 * n, None)
+                          _p(vel) if vel is not None else None, 3 * n,
+                          *[_p(e) if e is not None else None for e in errs])
         oc = opts.to_c()
         rc = self._lib.pp_solve_batch(self._h, qf.ctypes.data_as(_dp), nq, nq, ctypes.byref(oc), ctypes.byref(rv),
                                       info.ctypes.data_as(_ip))
@@ -247,21 +275,23 @@ class PhononContext:
         if z is not None:
             # per q the buffer holds z[2*(r + n*j)] (column-major) -> numpy (r, j)
             z = np.ascontiguousarray(z.transpose(0, 2, 1))
-        return Result(m=m, nz=nz, w=w, z=z, vel=vel, info=info)
-
+        return Result(m=m, nz=nz, w=w, z=z, vel=vel, info=info, resid=errs[0], werr=errs[1], zerr=errs[2])
 
     def solve_device(self, q_dev, opts: EigOpts, w_dev, m_dev, nz_dev, info_dev, vel_dev=None, z_dev=None,
-                     stream: int = 0) -> None:
+                     stream: int = 0, resid_dev=None, werr_dev=None, zerr_dev=None) -> None:
         """pp_solve_batch_device: q_dev (nq,3) float64 device tensor in Fortran
         order (q[t + nq*k]); outputs are device tensors sized like
         `Result`'s fields (w_dev (nq,n), vel_dev (nq,n,3), z_dev (nq,n,n)
-        complex128, m/nz/info (nq,) int64).  Enqueued on `stream`."""
+        complex128, m/nz/info (nq,) int64, the error estimates (nq,n)).
+        Enqueued on `stream`."""
         n = self.n
         nq = int(m_dev.shape[0])
+
+        def ptr(t):
+            return ctypes.cast(t.data_ptr(), _dp) if t is not None else None
         rv = PPResultView(ctypes.cast(m_dev.data_ptr(), _ip), ctypes.cast(nz_dev.data_ptr(), _ip),
-                          ctypes.cast(w_dev.data_ptr(), _dp), n,
-                          ctypes.cast(z_dev.data_ptr(), _dp) if z_dev is not None else None, n, 2 * n * n,
-                          ctypes.cast(vel_dev.data_ptr(), _dp) if vel_dev is not None else None, 3 * n, None)
+                          ctypes.cast(w_dev.data_ptr(), _dp), n, ptr(z_dev), n, 2 * n * n, ptr(vel_dev), 3 * n,
+                          ptr(resid_dev), ptr(werr_dev), ptr(zerr_dev))
         oc = opts.to_c()
         rc = self._lib.pp_solve_batch_device(self._h, ctypes.c_void_p(q_dev.data_ptr()), nq, nq, ctypes.byref(oc),
                                              ctypes.byref(rv), ctypes.c_void_p(info_dev.data_ptr()),
@@ -290,9 +320,11 @@ def solve_multi(contexts, cell, q, opts: EigOpts | None = None, want_z: bool = T
     z = np.zeros((nq, nmax, nmax), np.complex128) if (vecs and want_z) else None
     vel = np.zeros((nq, nmax, 3)) if opts.vel else None
     zv = z.view(np.float64) if z is not None else None
+    errs = [np.zeros((nq, nmax)) for _ in range(3)] if opts.want_resid else [None] * 3
     rv = PPResultView(m.ctypes.data_as(_ip), nz.ctypes.data_as(_ip), _p(w), nmax,
                       _p(zv) if zv is not None else None, nmax, 2 * nmax * nmax,
-                      _p(vel) if vel is not None else None, 3 * nmax, None)
+                      _p(vel) if vel is not None else None, 3 * nmax,
+                      *[_p(e) if e is not None else None for e in errs])
     handles = (ctypes.c_void_p * len(contexts))(*[c._h.value for c in contexts])
     oc = opts.to_c()
     rc = L.pp_solve_multi(handles, len(contexts), cell.ctypes.data_as(_ip), qf.ctypes.data_as(_dp), nq, nq,
@@ -301,7 +333,7 @@ def solve_multi(contexts, cell, q, opts: EigOpts | None = None, want_z: bool = T
         raise PPError(rc, "pp_solve_multi")
     if z is not None:
         z = np.ascontiguousarray(z.transpose(0, 2, 1))
-    return Result(m=m, nz=nz, w=w, z=z, vel=vel, info=info)
+    return Result(m=m, nz=nz, w=w, z=z, vel=vel, info=info, resid=errs[0], werr=errs[1], zerr=errs[2])
 
 
 def heevx_values_noalloc(a_ptr: int, lda: int, n: int, w_ptr: int, m_ptr: int, info_ptr: int, range: str = "A",
@@ -337,6 +369,14 @@ def kernel_timer_report() -> dict:
         k, n, ms = line.split()
         out[k] = (int(n), float(ms))
     return out
+
+
+def debug_stall_tc_wait(matrix: int, cycles: int) -> None:
+    """Test hook: make the next tensor-core trailing update of batch matrix
+    `matrix` give up its first wait after `cycles` SM clocks (-1 disarms)."""
+    rc = load().pp_debug_stall_tc_wait(int(matrix), int(cycles))
+    if rc != 0:
+        raise PPError(rc, "pp_debug_stall_tc_wait")
 
 
 def kernel_launches() -> int:

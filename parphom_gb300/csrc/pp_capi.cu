@@ -114,6 +114,7 @@ struct pp_ctx {
   // staging for host calls
   double *d_q = nullptr;
   double *d_w = nullptr, *d_z = nullptr, *d_vel = nullptr;
+  double *d_err = nullptr;  // [3][B][n] resid, werr, zerr staging
   int64_t *d_m = nullptr, *d_nz = nullptr, *d_info = nullptr;
   // extra streams for the other parts of a batch (forked from and joined to
   // the working stream with events, so that they are captured into the graph)
@@ -283,6 +284,7 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   add((void **)&c->vraw, 8 * (size_t)B * 3 * mcap);
   add((void **)&c->d_q, 8 * (size_t)B * 3);
   add((void **)&c->d_w, 8 * (size_t)B * n);
+  add((void **)&c->d_err, 8 * (size_t)3 * B * n);
   add((void **)&c->d_vel, 8 * (size_t)B * 3 * mcap);
   add((void **)&c->d_m, 8 * (size_t)B);
   add((void **)&c->d_nz, 8 * (size_t)B);
@@ -338,6 +340,7 @@ int check_opts(const pp_ctx *c, const pp_eig_opts *o) {
 EigWork view_of(const EigWork &w, int off, int cnt) {
   EigWork v = w;
   v.B = cnt;
+  v.boff = w.boff + off;
   auto sh = [off](void *p, size_t stride_bytes) -> void * {
     return p ? (void *)((char *)p + stride_bytes * (size_t)off) : nullptr;
   };
@@ -377,11 +380,21 @@ EigWork view_of(const EigWork &w, int off, int cnt) {
   return v;
 }
 
+// Eigenvectors are formed when asked for, for velocities, and for the error
+// estimates (which need the full vectors).
+bool needs_vectors(const pp_eig_opts *o) { return o->jobz == 'V' || o->vel || o->want_resid; }
+
+// Velocities without eigenvector output (and without error estimates) need
+// only the eigenvector rows of atoms in boundary blocks.
+bool rows_only_mode(const Geometry &g, const pp_eig_opts *o, bool want_z) {
+  return o->vel && !want_z && !o->want_resid && g.nbrows < g.n;
+}
+
 // Reduction, tridiagonal eigenpairs and back-transform of the matrices of w
 // on stream s.
 int eig_stages(pp_ctx *c, EigWork &w, const pp_eig_opts *o, bool want_z, cudaStream_t s) {
   const int prec = o->precision;
-  const bool vecs = o->jobz == 'V' || o->vel;
+  const bool vecs = needs_vectors(o);
   if (prec == PP_PREC_MIXED)
     TRY_CUDA(tridiagonalize<df>(w, s));
   else
@@ -391,7 +404,7 @@ int eig_stages(pp_ctx *c, EigWork &w, const pp_eig_opts *o, bool want_z, cudaStr
   if (vecs) {
     // Velocities without eigenvector output need only the eigenvector rows
     // of atoms in boundary blocks: back-transform those rows only.
-    const bool rows_only = o->vel && !want_z && c->g.nbrows < c->g.n;
+    const bool rows_only = rows_only_mode(c->g, o, want_z);
     if (prec == PP_PREC_MIXED) {
       TRY_CUDA(tridiag_eigenvectors<df>(w, s));
       if (rows_only)
@@ -461,7 +474,7 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
     if (r) return r;
   }
   if (o->vel) {
-    const bool rows_only = !want_z && c->g.nbrows < c->g.n;
+    const bool rows_only = rows_only_mode(c->g, o, want_z);
     if (rows_only)
       TRY_CUDA(velocities(c->g, c->d_q, B, w.Eb, w.nbr, (int64_t)w.nbr * w.mcap, prec == PP_PREC_MIXED ? 1 : 0,
                           w.rng, w.mcap, o->vel_method, c->vraw, c->vpart, c->nsplit, c->g.d_rowmap, s));
@@ -481,11 +494,12 @@ bool graphs_enabled() {
 // the batch size, the options and the workspace, so it is captured once and
 // replayed (one graph launch instead of ~6 launches per matrix column).
 int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
-  if (!graphs_enabled() || pp::kt_mask) return run_batch(c, B, o, mcap, want_z);
+  // (an armed test stall is a one-shot launch parameter: never captured)
+  if (!graphs_enabled() || pp::kt_mask || tc_stall_armed()) return run_batch(c, B, o, mcap, want_z);
   char key[160];
-  snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d|%d", c->ws, B, o->precision, o->jobz,
-           o->range, o->vel_method, o->vel, (long long)o->il, (long long)o->iu, o->vl, o->vu, o->abstol,
-           want_z ? 1 : 0, split_ways());
+  snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d|%d|%d", c->ws, B, o->precision,
+           o->jobz, o->range, o->vel_method, o->vel, (long long)o->il, (long long)o->iu, o->vl, o->vu, o->abstol,
+           want_z ? 1 : 0, split_ways(), o->want_resid ? 1 : 0);
   cudaStream_t s = c->stream;
   if (c->gexec && strcmp(key, c->gkey) == 0) {
     TRY_CUDA(cudaGraphLaunch(c->gexec, s));
@@ -541,11 +555,76 @@ int pick_batch(pp_ctx *c, int64_t nq, int mcap) {
   return std::max(B, 1);
 }
 
+// Boundary blocks (I < J, tie set with a non-home image, Phi block
+// non-zero) and the rows of their atoms, from the current Phi and tie sets;
+// replaces any earlier tables.
+int build_boundary_tables(pp_ctx *c) {
+  Geometry &g = c->g;
+  const int64_t N = g.natom, n = g.n;
+  cudaStream_t s = c->stream;
+  for (void *p : {(void *)g.d_bnd, (void *)g.d_bndmask, (void *)g.d_brows, (void *)g.d_rowmap})
+    if (p) cudaFree(p);
+  g.d_bnd = nullptr;
+  g.d_bndmask = nullptr;
+  g.d_brows = nullptr;
+  g.d_rowmap = nullptr;
+  g.nbnd = g.nbrows = 0;
+  uint8_t *d_flags = nullptr;
+  if (cudaMalloc(&d_flags, (size_t)N * N) != cudaSuccess) return PP_ERR_NOMEM;
+  geom_block_nonzero(g, d_flags, s);
+  std::vector<uint8_t> flags_h((size_t)N * N);
+  std::vector<uint16_t> mask_h((size_t)N * N);
+  cudaMemcpyAsync(flags_h.data(), d_flags, (size_t)N * N, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(mask_h.data(), g.d_mask, sizeof(uint16_t) * N * N, cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  cudaFree(d_flags);
+  if (e != cudaSuccess) return cuda_err(e);
+  std::vector<int2> bnd;
+  std::vector<uint16_t> bmask;
+  for (int64_t I = 0; I < N; ++I)
+    for (int64_t J = I + 1; J < N; ++J) {
+      const uint16_t m = mask_h[I + N * J];
+      if ((m & ~(1u << 4)) && flags_h[I + N * J]) {
+        bnd.push_back(make_int2((int)I, (int)J));
+        bmask.push_back(m);
+      }
+    }
+  g.nbnd = (int64_t)bnd.size();
+  // rows of the atoms that appear in boundary blocks (all the velocity
+  // kernel reads of the eigenvectors)
+  std::vector<int> rows, rowmap(n, -1);
+  {
+    std::vector<char> used(N, 0);
+    for (auto &p : bnd) used[p.x] = used[p.y] = 1;
+    for (int64_t I = 0; I < N; ++I)
+      if (used[I])
+        for (int a = 0; a < 3; ++a) {
+          rowmap[3 * I + a] = (int)rows.size();
+          rows.push_back((int)(3 * I + a));
+        }
+  }
+  g.nbrows = (int64_t)rows.size();
+  if (cudaMalloc(&g.d_rowmap, sizeof(int) * n) != cudaSuccess) return PP_ERR_NOMEM;
+  cudaMemcpy(g.d_rowmap, rowmap.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+  if (g.nbrows) {
+    if (cudaMalloc(&g.d_brows, sizeof(int) * g.nbrows) != cudaSuccess) return PP_ERR_NOMEM;
+    cudaMemcpy(g.d_brows, rows.data(), sizeof(int) * g.nbrows, cudaMemcpyHostToDevice);
+  }
+  if (g.nbnd) {
+    if (cudaMalloc(&g.d_bnd, sizeof(int2) * g.nbnd) != cudaSuccess) return PP_ERR_NOMEM;
+    if (cudaMalloc(&g.d_bndmask, sizeof(uint16_t) * g.nbnd) != cudaSuccess) return PP_ERR_NOMEM;
+    cudaMemcpy(g.d_bnd, bnd.data(), sizeof(int2) * g.nbnd, cudaMemcpyHostToDevice);
+    cudaMemcpy(g.d_bndmask, bmask.data(), sizeof(uint16_t) * g.nbnd, cudaMemcpyHostToDevice);
+  }
+  const cudaError_t e2 = cudaGetLastError();
+  return e2 == cudaSuccess ? PP_OK : cuda_err(e2);
+}
+
 }  // namespace
 
 extern "C" {
 
-int64_t pp_version(void) { return 100; }
+int64_t pp_version(void) { return 20000; }
 
 int64_t pp_kernel_launches(void) { return pp::g_launches.load(); }
 
@@ -570,6 +649,13 @@ int pp_ktimer_enable(const char *names) {
     pp::kt_ms[k] = 0.0;
   }
   pp::kt_mask = mask;
+  return PP_OK;
+}
+
+int pp_debug_stall_tc_wait(int64_t matrix, int64_t cycles) {
+  if (matrix < -1) return -1;
+  if (cycles < 0 || cycles > 2000000000LL) return -2;
+  pp::arm_tc_stall(matrix, (long long)cycles);
   return PP_OK;
 }
 
@@ -683,57 +769,41 @@ int pp_ctx_create(const pp_system *sys, const double *fc, int64_t ldfc, int64_t 
   cudaMemcpyAsync(g.d_mass, mass_atom.data(), sizeof(double) * N, cudaMemcpyHostToDevice, s);
   if (geom_symmetrize_fc(g, (flags & PP_FLAG_ENFORCE_ASR) ? 1 : 0, s) != cudaSuccess) return fail(PP_ERR_CUDA);
   if (geom_build_masks(g, s) != cudaSuccess) return fail(PP_ERR_CUDA);
-  // boundary blocks: I < J, tie set with a non-home image, Phi block non-zero
-  uint8_t *d_flags = nullptr;
-  if (cudaMalloc(&d_flags, (size_t)N * N) != cudaSuccess) return fail(PP_ERR_NOMEM);
-  geom_block_nonzero(g, d_flags, s);
-  std::vector<uint8_t> flags_h((size_t)N * N);
-  std::vector<uint16_t> mask_h((size_t)N * N);
-  cudaMemcpyAsync(flags_h.data(), d_flags, (size_t)N * N, cudaMemcpyDeviceToHost, s);
-  cudaMemcpyAsync(mask_h.data(), g.d_mask, sizeof(uint16_t) * N * N, cudaMemcpyDeviceToHost, s);
-  cudaError_t e = cudaStreamSynchronize(s);
-  cudaFree(d_flags);
-  if (e != cudaSuccess) return fail(cuda_err(e));
-  std::vector<int2> bnd;
-  std::vector<uint16_t> bmask;
-  for (int64_t I = 0; I < N; ++I)
-    for (int64_t J = I + 1; J < N; ++J) {
-      const uint16_t m = mask_h[I + N * J];
-      if ((m & ~(1u << 4)) && flags_h[I + N * J]) {
-        bnd.push_back(make_int2((int)I, (int)J));
-        bmask.push_back(m);
-      }
-    }
-  g.nbnd = (int64_t)bnd.size();
-  // rows of the atoms that appear in boundary blocks (all the velocity
-  // kernel reads of the eigenvectors)
-  std::vector<int> rows, rowmap(n, -1);
   {
-    std::vector<char> used(N, 0);
-    for (auto &p : bnd) used[p.x] = used[p.y] = 1;
-    for (int64_t I = 0; I < N; ++I)
-      if (used[I])
-        for (int a = 0; a < 3; ++a) {
-          rowmap[3 * I + a] = (int)rows.size();
-          rows.push_back((int)(3 * I + a));
-        }
+    const int rb = build_boundary_tables(c);
+    if (rb) return fail(rb);
   }
-  g.nbrows = (int64_t)rows.size();
-  if (cudaMalloc(&g.d_rowmap, sizeof(int) * n) != cudaSuccess) return fail(PP_ERR_NOMEM);
-  cudaMemcpy(g.d_rowmap, rowmap.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
-  if (g.nbrows) {
-    if (cudaMalloc(&g.d_brows, sizeof(int) * g.nbrows) != cudaSuccess) return fail(PP_ERR_NOMEM);
-    cudaMemcpy(g.d_brows, rows.data(), sizeof(int) * g.nbrows, cudaMemcpyHostToDevice);
-  }
-  if (g.nbnd) {
-    if (cudaMalloc(&g.d_bnd, sizeof(int2) * g.nbnd) != cudaSuccess) return fail(PP_ERR_NOMEM);
-    if (cudaMalloc(&g.d_bndmask, sizeof(uint16_t) * g.nbnd) != cudaSuccess) return fail(PP_ERR_NOMEM);
-    cudaMemcpy(g.d_bnd, bnd.data(), sizeof(int2) * g.nbnd, cudaMemcpyHostToDevice);
-    cudaMemcpy(g.d_bndmask, bmask.data(), sizeof(uint16_t) * g.nbnd, cudaMemcpyHostToDevice);
-  }
+  cudaError_t e = cudaSuccess;
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(cuda_err(e));
   *out = c;
+  return PP_OK;
+}
+
+int pp_ctx_update_fc(pp_ctx *c, const double *fc, int64_t ldfc, int64_t flags, int32_t fc_on_device) {
+  if (!c) return -1;
+  if (c->broken) return PP_ERR_STATE;
+  if (!fc) return -2;
+  const int64_t n = c->g.n;
+  if (ldfc < n) return -3;
+  if (fc_on_device != 0 && fc_on_device != 1) return -5;
+  if (!fc_on_device)
+    for (int64_t cc = 0; cc < n; ++cc)
+      for (int64_t r = 0; r <= cc; ++r)
+        if (!std::isfinite(fc[r + ldfc * cc])) return PP_ERR_NAN;
+  cudaStream_t s = c->stream;
+  TRY_CUDA(cudaStreamSynchronize(s));
+  TRY_CUDA(cudaMemcpy2DAsync(c->g.d_fc, sizeof(double) * n, fc, sizeof(double) * ldfc, sizeof(double) * n, n,
+                             fc_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  TRY_CUDA(geom_symmetrize_fc(c->g, (flags & PP_FLAG_ENFORCE_ASR) ? 1 : 0, s));
+  // the boundary tables follow Phi's non-zero blocks; a captured graph holds
+  // the old tables' addresses and counts
+  drop_graph(c);
+  const int r = build_boundary_tables(c);
+  if (r) {
+    c->broken = 1;
+    return r;
+  }
   return PP_OK;
 }
 
@@ -802,6 +872,11 @@ int pp_solve_batch(pp_ctx *c, const double *q, int64_t ldq, int64_t nq, const pp
     TRY_CUDA(finalize_outputs(c->w, o->precision == PP_PREC_MIXED ? 1 : 0, o->raw_lambda, c->vraw, o->vel ? 1 : 0,
                               0, c->d_w, n, nullptr, 0, 0, c->d_vel, 3 * (int64_t)c->w.mcap, c->d_m, c->d_nz, c->d_info,
                               vecs ? 1 : 0, s));
+    const bool errs = o->want_resid && (out->resid || out->werr || out->zerr);
+    double *e_res = c->d_err, *e_w = c->d_err + (size_t)B * n, *e_z = c->d_err + 2 * (size_t)B * n;
+    if (errs)
+      TRY_CUDA(error_estimates(c->g, c->d_q, c->w, o->precision == PP_PREC_MIXED ? 1 : 0, o->raw_lambda, c->vpart,
+                               e_res, e_w, e_z, n, s));
     TRY_CUDA(cudaMemcpyAsync(mh.data(), c->d_m, 8 * Bb, cudaMemcpyDeviceToHost, s));
     TRY_CUDA(cudaMemcpyAsync(nzh.data(), c->d_nz, 8 * Bb, cudaMemcpyDeviceToHost, s));
     TRY_CUDA(cudaMemcpyAsync(infoh.data(), c->d_info, 8 * Bb, cudaMemcpyDeviceToHost, s));
@@ -818,11 +893,20 @@ int pp_solve_batch(pp_ctx *c, const double *q, int64_t ldq, int64_t nq, const pp
         if (o->vel && out->vel)
           TRY_CUDA(cudaMemcpyAsync(out->vel + out->velstride * t, c->d_vel + 3 * (int64_t)c->w.mcap * b,
                                    sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, s));
+        if (errs) {
+          const double *src[3] = {e_res, e_w, e_z};
+          double *dst[3] = {out->resid, out->werr, out->zerr};
+          for (int f = 0; f < 3; ++f)
+            if (dst[f])
+              TRY_CUDA(cudaMemcpyAsync(dst[f] + out->ldw * t, src[f] + n * b, sizeof(double) * m,
+                                       cudaMemcpyDeviceToHost, s));
+        }
       }
     }
     if (want_z) {
       // eigenvectors: convert to FP64 complex in the A buffer (free after the
-      // back-transform), then copy each matrix with the caller's pitch.
+      // back-transform and the error estimates), then copy each matrix with
+      // the caller's pitch.
       double *zst = (double *)c->w.A;
       TRY_CUDA(finalize_outputs(c->w, o->precision == PP_PREC_MIXED ? 1 : 0, o->raw_lambda, c->vraw, 0, 1, nullptr,
                                 0, zst, c->w.lda, 2 * c->w.sA, nullptr, 0, nullptr, nullptr, nullptr, 1, s));
@@ -890,6 +974,11 @@ int pp_solve_batch_device(pp_ctx *c, const double *q_dev, int64_t ldq, int64_t n
                                   want_z ? out->z + out->zstride * t0 : nullptr, out->ldz, out->zstride,
                                   out->vel ? out->vel + out->velstride * t0 : nullptr, out->velstride, out->m + t0,
                                   out->nz + t0, info_dev ? info_dev + t0 : nullptr, vecs ? 1 : 0, s));
+    if (!r && o->want_resid && (out->resid || out->werr || out->zerr))
+      r = cuda_err(error_estimates(c->g, c->d_q, c->w, o->precision == PP_PREC_MIXED ? 1 : 0, o->raw_lambda,
+                                   c->vpart, out->resid ? out->resid + out->ldw * t0 : nullptr,
+                                   out->werr ? out->werr + out->ldw * t0 : nullptr,
+                                   out->zerr ? out->zerr + out->ldw * t0 : nullptr, out->ldw, s));
     if (r) {
       c->stream = saved;
       return r;
@@ -986,7 +1075,7 @@ int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const
   const bool vecs = o->jobz == 'V' || o->vel;
   const bool want_z = vecs && out->z;
   if (want_z && out->ldz < nmax) return -8;
-  bool rows_only = o->vel && !want_z;
+  bool rows_only = o->vel && !want_z && !o->want_resid;
   for (int64_t k = 0; k < nctx; ++k) rows_only = rows_only && ctxs[k]->g.nbrows < ctxs[k]->g.n;
   pp_ctx *h = ctxs[0];
   const int mcap = o->range == 'I' ? (int)(o->iu - o->il + 1) : (int)nmax;
@@ -1042,7 +1131,7 @@ int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const
       TRY_CUDA(tridiagonalize<double>(w, s));
     TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s,
                                  prec == PP_PREC_MIXED));
-    if (vecs) {
+    if (needs_vectors(o)) {
       if (prec == PP_PREC_MIXED)
         TRY_CUDA(tridiag_eigenvectors<df>(w, s));
       else
@@ -1074,6 +1163,15 @@ int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const
     }
     TRY_CUDA(finalize_outputs(w, fmt, o->raw_lambda, h->vraw, o->vel ? 1 : 0, 0, h->d_w, nmax, nullptr, 0, 0, h->d_vel,
                               3 * (int64_t)w.mcap, h->d_m, h->d_nz, h->d_info, vecs ? 1 : 0, s));
+    const bool errs = o->want_resid && (out->resid || out->werr || out->zerr);
+    double *e_res = h->d_err, *e_w = h->d_err + (size_t)B * nmax, *e_z = h->d_err + 2 * (size_t)B * nmax;
+    if (errs)
+      for (auto &g : segs) {
+        EigWork v = view_of(w, g.off, g.cnt);
+        const size_t o0 = (size_t)g.off * nmax;
+        TRY_CUDA(error_estimates(g.c->g, h->d_q + 3 * g.off, v, fmt, o->raw_lambda, h->vpart, e_res + o0, e_w + o0,
+                                 e_z + o0, nmax, s));
+      }
     TRY_CUDA(cudaMemcpyAsync(mh.data(), h->d_m, 8 * Bb, cudaMemcpyDeviceToHost, s));
     TRY_CUDA(cudaMemcpyAsync(nzh.data(), h->d_nz, 8 * Bb, cudaMemcpyDeviceToHost, s));
     TRY_CUDA(cudaMemcpyAsync(infoh.data(), h->d_info, 8 * Bb, cudaMemcpyDeviceToHost, s));
@@ -1089,6 +1187,14 @@ int pp_solve_multi(pp_ctx *const *ctxs, int64_t nctx, const int64_t *cell, const
         if (o->vel && out->vel)
           TRY_CUDA(cudaMemcpyAsync(out->vel + out->velstride * t, h->d_vel + 3 * (int64_t)w.mcap * b,
                                    sizeof(double) * 3 * mh[b], cudaMemcpyDeviceToHost, s));
+        if (errs) {
+          const double *src[3] = {e_res, e_w, e_z};
+          double *dst[3] = {out->resid, out->werr, out->zerr};
+          for (int f = 0; f < 3; ++f)
+            if (dst[f])
+              TRY_CUDA(cudaMemcpyAsync(dst[f] + out->ldw * t, src[f] + nmax * b, sizeof(double) * mh[b],
+                                       cudaMemcpyDeviceToHost, s));
+        }
       }
     }
     if (want_z) {

@@ -120,6 +120,103 @@ __global__ void k_sum_rows(const double *p, int64_t ne, int64_t nb, double scale
 
 int cerr(cudaError_t e) { return e == cudaSuccess ? PP_OK : (e == cudaErrorMemoryAllocation ? PP_ERR_NOMEM : PP_ERR_CUDA); }
 
+// ---- device-resident forms: every array in device memory, no scratch.
+// One thread per band, one block row per energy; the block's bands are
+// summed in shared memory and added to the energy's total (zeroed first).
+constexpr int DV_NT = 128;
+
+__device__ __forceinline__ double block_sum128(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < DV_NT / 32; ++k) r += sh[k];
+  return r;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(DV_NT) k_dos_tri_dev(const double *freq, int64_t ldf, const double *func,
+                                                       int64_t ldfunc, int64_t nbands, const int64_t *tri,
+                                                       int64_t ntri, const double *E, int64_t ne, double *dos,
+                                                       double *nd) {
+  __shared__ double sh[2][DV_NT / 32];
+  const int64_t k = (int64_t)blockIdx.x * DV_NT + threadIdx.x;  // band
+  const int64_t i = blockIdx.y;                                 // energy
+  if (i >= ne) return;
+  const double Ef = E[i];
+  double sd = 0.0, sn = 0.0;
+  if (k < nbands) {
+    for (int64_t j = 0; j < ntri; ++j) {
+      double a[4][2];
+      a[0][0] = Ef;
+      a[0][1] = 0.0;
+      for (int v = 0; v < 3; ++v) {
+        const int64_t q = tri[3 * j + v];
+        a[v + 1][0] = freq[q * ldf + k];
+        a[v + 1][1] = func ? func[q * ldfunc + k] : 1.0;
+      }
+      for (int p = 0; p < 4; ++p)  // exchange sort of bz_integration.f90:50-65
+        for (int r = p + 1; r < 4; ++r)
+          if (a[p][0] > a[r][0]) {
+            const double t0 = a[p][0], t1 = a[p][1];
+            a[p][0] = a[r][0];
+            a[p][1] = a[r][1];
+            a[r][0] = t0;
+            a[r][1] = t1;
+          }
+      double d, n;
+      integrate_triangle(a, Ef, d, n);
+      sd += d;
+      sn += n;
+    }
+  }
+  sd = block_sum128(sd, sh[0]);
+  sn = block_sum128(sn, sh[1]);
+  if (threadIdx.x == 0) {
+    atomicAdd(&dos[i], sd);
+    atomicAdd(&nd[i], sn);
+  }
+}
+
+__global__ void __launch_bounds__(DV_NT) k_dos_smear_dev(int method, const double *freq, int64_t ldf, int64_t nq,
+                                                         int64_t nbands, const double *weights, double width,
+                                                         const double *E, int64_t ne, double scale, double *dos) {
+  __shared__ double sh[DV_NT / 32];
+  const int64_t k = (int64_t)blockIdx.x * DV_NT + threadIdx.x;
+  const int64_t i = blockIdx.y;
+  if (i >= ne) return;
+  const double e = E[i];
+  double s = 0.0;
+  if (k < nbands) {
+    for (int64_t q = 0; q < nq; ++q) {
+      const double e0 = freq[q * ldf + k];
+      double d;
+      if (method == 1) {
+        const double x = (e - e0) / width;
+        d = exp(-(x * x) / 2) / (sqrt(2 * PI_REF) * width);
+      } else {
+        const double h = width / 2;
+        d = (h / ((e - e0) * (e - e0) + h * h)) * (1 / PI_REF);
+      }
+      s += d * weights[q];
+    }
+  }
+  s = block_sum128(s, sh);
+  if (threadIdx.x == 0) atomicAdd(&dos[i], s * scale);
+}
+
+// func[q ldfunc + j] = v_a v_b of mode j at q-point q (a = b = -1: |v|^2),
+// from the velocity output vel[q velstride + 3 j + d].
+__global__ void k_vel_weights(const double *vel, int64_t velstride, int64_t nq, int64_t nbands, int a, int b,
+                              double *func, int64_t ldfunc) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t q = blockIdx.y;
+  if (j >= nbands || q >= nq) return;
+  const double *v = vel + q * velstride + 3 * j;
+  func[q * ldfunc + j] = (a < 0) ? v[0] * v[0] + v[1] * v[1] + v[2] * v[2] : v[a] * v[b];
+}
+
 }  // namespace
 
 extern "C" PP_API int pp_dos_triangulation(const double *freq, int64_t ldf, int64_t nk, int64_t nbands,
@@ -210,4 +307,77 @@ extern "C" PP_API int pp_dos_smearing(int32_t method, const double *freq, int64_
   for (void *p : {(void *)dfreq, (void *)dw, (void *)dE, (void *)pd, (void *)od})
     if (p) cudaFree(p);
   return cerr(e);
+}
+
+extern "C" PP_API int pp_dos_triangulation_device(const double *freq_dev, int64_t ldf, int64_t nk, int64_t nbands,
+                                                  const double *func_dev, int64_t ldfunc, const int64_t *tri_dev,
+                                                  int64_t ntri, const double *energy_dev, int64_t ne, double *dos_dev,
+                                                  double *nd_dev, void *stream) {
+  if (!freq_dev) return -1;
+  if (ldf < nbands) return -2;
+  if (nk < 1) return -3;
+  if (nbands < 1) return -4;
+  if (func_dev && ldfunc < nbands) return -6;
+  if (!tri_dev && ntri > 0) return -7;
+  if (ntri < 0) return -8;
+  if (!energy_dev && ne > 0) return -9;
+  if (ne < 0) return -10;
+  if (!dos_dev) return -11;
+  if (!nd_dev) return -12;
+  if (ne == 0) return PP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(dos_dev, 0, sizeof(double) * ne, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(nd_dev, 0, sizeof(double) * ne, s);
+  if (e == cudaSuccess) {
+    k_dos_tri_dev<<<dim3((unsigned)((nbands + DV_NT - 1) / DV_NT), (unsigned)ne), DV_NT, 0, s>>>(
+        freq_dev, ldf, func_dev, ldfunc, nbands, tri_dev, ntri, energy_dev, ne, dos_dev, nd_dev);
+    pp::count_launch(1);
+    e = cudaGetLastError();
+  }
+  return cerr(e);
+}
+
+extern "C" PP_API int pp_dos_smearing_device(int32_t method, const double *freq_dev, int64_t ldf, int64_t nq,
+                                             int64_t nbands, const double *weights_dev, double width,
+                                             const double *energy_dev, int64_t ne, int64_t natom, double *dos_dev,
+                                             void *stream) {
+  if (method != 1 && method != 2) return -1;
+  if (!freq_dev) return -2;
+  if (ldf < nbands) return -3;
+  if (nq < 1) return -4;
+  if (nbands < 1) return -5;
+  if (!weights_dev) return -6;
+  if (!(width > 0.0)) return -7;
+  if (!energy_dev && ne > 0) return -8;
+  if (ne < 0) return -9;
+  if (natom < 1) return -10;
+  if (!dos_dev) return -11;
+  if (ne == 0) return PP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(dos_dev, 0, sizeof(double) * ne, s);
+  if (e == cudaSuccess) {
+    k_dos_smear_dev<<<dim3((unsigned)((nbands + DV_NT - 1) / DV_NT), (unsigned)ne), DV_NT, 0, s>>>(
+        method, freq_dev, ldf, nq, nbands, weights_dev, width, energy_dev, ne, 1.0 / (double)natom, dos_dev);
+    pp::count_launch(1);
+    e = cudaGetLastError();
+  }
+  return cerr(e);
+}
+
+extern "C" PP_API int pp_velocity_weights_device(const double *vel_dev, int64_t velstride, int64_t nq, int64_t nbands,
+                                                 int32_t a, int32_t b, double *func_dev, int64_t ldfunc,
+                                                 void *stream) {
+  if (!vel_dev) return -1;
+  if (velstride < 3 * nbands) return -2;
+  if (nq < 0) return -3;
+  if (nbands < 1) return -4;
+  if (!((a == -1 && b == -1) || (a >= 0 && a < 3 && b >= 0 && b < 3))) return -5;
+  if (!func_dev) return -7;
+  if (ldfunc < nbands) return -8;
+  if (nq == 0) return PP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_vel_weights<<<dim3((unsigned)((nbands + 127) / 128), (unsigned)nq), 128, 0, s>>>(vel_dev, velstride, nq, nbands,
+                                                                                     a, b, func_dev, ldfunc);
+  pp::count_launch(1);
+  return cerr(cudaGetLastError());
 }

@@ -43,6 +43,7 @@ void kt_end(int k, cudaStream_t s);
 // z64 for the FP64 form, zdf for the double-float form.
 struct EigWork {
   int B = 0;           // matrices in the batch
+  int boff = 0;        // index of the first matrix in the whole batch (views)
   int nmax = 0;        // largest order
   int mcap = 0;        // eigenvector columns allocated per matrix
   int nb = 32;         // panel width
@@ -163,6 +164,10 @@ size_t her2k_tc_bytes(int64_t nmax);
 int64_t her2k_tc_exps(int64_t nmax);
 cudaError_t prepare_her2k_tc();
 bool tc_enabled();
+// Test hook: the next tensor-core trailing update that covers batch matrix
+// `matrix` makes its first wait give up after `cycles` SM clocks.
+void arm_tc_stall(int64_t matrix, long long cycles);
+bool tc_stall_armed();
 cudaError_t prepare_bisect(size_t bytes);
 // dynamic shared memory of the bisection kernel for order n (0: global-memory mode)
 size_t bisect_smem(int64_t n, int mixed);
@@ -175,6 +180,12 @@ cudaError_t back_transform(EigWork &w, cudaStream_t s);
 // Rows `rows` of E = Q Z only: X = Q^H P^T (P selects the rows), Eb = X^H Z.
 template <class R>
 cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaStream_t s);
+
+// Per-eigenpair error estimates (residual, eigenvalue and eigenvector error
+// bounds) of the eigenpairs in w (full eigenvectors in w.E), FP64; D(q) is
+// assembled again into w.A.  sums: 3 * B * mcap doubles of scratch.
+cudaError_t error_estimates(const Geometry &g, const double *d_q, EigWork &w, int efmt, int raw_lambda,
+                            double *sums, double *resid, double *werr, double *zerr, int64_t ldw, cudaStream_t s);
 
 // Output conversion
 cudaError_t finalize_outputs(EigWork &w, int efmt, int raw_lambda, const double *d_vraw, int want_vel, int want_z,

@@ -190,6 +190,11 @@ struct TcUpdate {
   int ncols_fixed;  // columns: ncols_fixed, or n_b - cbase when 0; rows: n_b - rbase
   int tri, nprod;
   TcOperand x[2], y[2];
+  // test hook (pp_debug_stall_tc_wait): matrix stall_b's first CTA waits,
+  // before its first row-operand wait, on an mbarrier that nothing arrives
+  // on, for stall_cycles SM clocks, and so takes the time-out path; -1: off
+  int stall_b;
+  long long stall_cycles;
 };
 
 __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nvec, int *err) {
@@ -198,11 +203,12 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   uint8_t *sBop = smem + TC_OP;                          // two column-operand buffers
   int *sEc = (int *)(smem + TC_OP + 2 * TC_BBYTES);      // two x 64 column exponents
   // mbarriers: [0] row operand landed (waited by thread 0), [1], [2] column
-  // buffer 0 / 1 landed, [3] MMAs of the block done.
+  // buffer 0 / 1 landed, [3] MMAs of the block done, [4] never arrived on
+  // (the test hook's wait).
   // Each barrier a thread waits on completes exactly once between two of
   // its waits, so parity waits cannot skip a phase.
   uint64_t *bars = (uint64_t *)(smem + TC_OP + 2 * TC_BBYTES + 512);
-  uint32_t *tslot = (uint32_t *)(bars + 4);
+  uint32_t *tslot = (uint32_t *)(bars + 5);
   const int b = blockIdx.z, R = blockIdx.y, q = blockIdx.x;
   const int n = nvec[b];
   const int nrows = n - u.rbase;
@@ -222,13 +228,14 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) tc::tmem_alloc(tslot, 512);
   if (tid == 0) {
-    for (int i = 0; i < 4; ++i) tc::mbar_init(&bars[i], 1);
+    for (int i = 0; i < 5; ++i) tc::mbar_init(&bars[i], 1);
     tc::mbar_init_fence();
   }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t tm = *tslot;
+  const bool stall = b == u.stall_b && R == 0 && q == 0;
   zdf *C = u.C + b * u.sC;
   const int r0 = u.rbase + 128 * R;  // first global row of this row block
   const int nr = min(128, nrows - 128 * R);
@@ -273,7 +280,8 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
         for (int c = c0; c < min(c0 + 32, u.cbase + ncols); ++c)
           tc::prefetch_l2(C + r0 + u.ldc * c, (uint32_t)nr * 16u);
       }
-      if (i % ncbw == 0) good = tc::mbar_wait(&bars[0], (uint32_t)p);
+      if (i == 0 && stall) good = tc::mbar_wait(&bars[4], 0u, u.stall_cycles);
+      if (i % ncbw == 0) good = good && tc::mbar_wait(&bars[0], (uint32_t)p);
       good = good && tc::mbar_wait(&bars[1 + (i & 1)], (uint32_t)((i >> 1) & 1));
       if (good) {
         tc::fence_after();
@@ -342,16 +350,18 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   }
   if (!ok) {
     // let the copies and MMAs still in flight finish (bounded waits) before
-    // the shared and tensor memory are released
-    if (tid == 0) {
-      tc::mbar_wait(&bars[0], 0, 200000000LL);
-      if (failed_i >= 0) {
-        tc::mbar_wait(&bars[3], (uint32_t)(failed_i & 1), 200000000LL);
-        const int nx = failed_i + 1;
-        if (nx < nblk) tc::mbar_wait(&bars[1 + (nx & 1)], (uint32_t)((nx >> 1) & 1), 200000000LL);
-      }
-      atomicExch(&err[b], 1);
+    // the shared and tensor memory are released: the row operand of the
+    // failed step's product, the failed step's MMAs and column copy, and the
+    // column copy issued for the step after it
+    if (tid == 0 && failed_i >= 0) {
+      const int fp = failed_i / ncbw;
+      tc::mbar_wait(&bars[0], (uint32_t)(fp & 1), 200000000LL);
+      tc::mbar_wait(&bars[3], (uint32_t)(failed_i & 1), 200000000LL);
+      tc::mbar_wait(&bars[1 + (failed_i & 1)], (uint32_t)((failed_i >> 1) & 1), 200000000LL);
+      const int nx = failed_i + 1;
+      if (nx < nblk) tc::mbar_wait(&bars[1 + (nx & 1)], (uint32_t)((nx >> 1) & 1), 200000000LL);
     }
+    if (tid == 0) atomicExch(&err[b], 1);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
@@ -696,6 +706,32 @@ cudaError_t launch_slices(const TcSliceSrc &src, int rows_max, EigWork &w, int k
 }
 }  // namespace
 
+// One-shot stall of the test hook: the global batch index of the matrix
+// and the wait's limit in SM clocks (-1: not armed).
+static std::mutex g_stall_mu;
+static int64_t g_stall_matrix = -1;
+static long long g_stall_cycles = 0;
+
+void arm_tc_stall(int64_t matrix, long long cycles) {
+  std::lock_guard<std::mutex> g(g_stall_mu);
+  g_stall_matrix = matrix;
+  g_stall_cycles = cycles;
+}
+bool tc_stall_armed() {
+  std::lock_guard<std::mutex> g(g_stall_mu);
+  return g_stall_matrix >= 0;
+}
+// The stall for a launch over batch matrices [boff, boff + B): consumed by
+// the first launch that covers the armed matrix.
+static int take_stall(const EigWork &w, long long *cycles) {
+  std::lock_guard<std::mutex> g(g_stall_mu);
+  if (g_stall_matrix < w.boff || g_stall_matrix >= (int64_t)w.boff + w.B) return -1;
+  const int b = (int)(g_stall_matrix - w.boff);
+  *cycles = g_stall_cycles;
+  g_stall_matrix = -1;
+  return b;
+}
+
 // A(k1:n, k1:n) -= V W^H + W V^H, lower triangle (panel k0 of width jb).
 cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s) {
   const int k1 = k0 + jb;
@@ -722,6 +758,7 @@ cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s) {
   u.y[0] = Wo;
   u.x[1] = Wo;
   u.y[1] = V;
+  u.stall_b = take_stall(w, &u.stall_cycles);
   const int nrb = (mmax + 127) / 128;
   const int nq = (4 * nrb + TC_CB - 1) / TC_CB;
   PP_KT(KT_HER2K, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>(u, w.nvec, w.tcErr)));
@@ -753,6 +790,7 @@ cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t s
   u.ncols_fixed = ncols;
   u.tri = 0;
   u.nprod = 1;
+  u.stall_b = -1;
   u.x[0] = TcOperand{w.tcS, w.sTcS, TC_OP, w.tcE, w.sTcE, 1, 0};
   u.y[0] = TcOperand{w.tcS + vbl, w.sTcS, TC_OP, w.tcE + yexp, w.sTcE, 1, 0};
   u.x[1] = u.x[0];

@@ -33,6 +33,14 @@ def _lib():
         L.pp_dos_smearing.argtypes = [ctypes.c_int32, _dp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _dp,
                                       ctypes.c_double, _dp, ctypes.c_int64, ctypes.c_int64, _dp]
         L.pp_dos_smearing.restype = ctypes.c_int
+        vp, i64 = ctypes.c_void_p, ctypes.c_int64
+        L.pp_dos_triangulation_device.argtypes = [vp, i64, i64, i64, vp, i64, vp, i64, vp, i64, vp, vp, vp]
+        L.pp_dos_triangulation_device.restype = ctypes.c_int
+        L.pp_dos_smearing_device.argtypes = [ctypes.c_int32, vp, i64, i64, i64, vp, ctypes.c_double, vp, i64, i64,
+                                             vp, vp]
+        L.pp_dos_smearing_device.restype = ctypes.c_int
+        L.pp_velocity_weights_device.argtypes = [vp, i64, i64, i64, ctypes.c_int32, ctypes.c_int32, vp, i64, vp]
+        L.pp_velocity_weights_device.restype = ctypes.c_int
         L._dos_bound = True
     return L
 
@@ -89,3 +97,55 @@ def smearing_dos(freq, weights, energy, width, natom, method="gaussian"):
     if rc != 0:
         raise api.PPError(rc, "pp_dos_smearing")
     return out
+
+
+# ---- device-resident forms (torch tensors in, torch tensors out) ----------
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def linear_triangulation_device(freq_dev, tri_dev, energy_dev, nbands=None, func_dev=None, stream=0):
+    """Raw per-triangle sums (dos, nd) on the device.  freq_dev (nk, ldf) and
+    func_dev (nk, ldfunc) float64 rows per q-point, e.g. the w output of
+    PhononContext.solve_device; the first `nbands` columns are used."""
+    import torch
+    nk, ldf = freq_dev.shape
+    nb = ldf if nbands is None else int(nbands)
+    ne = int(energy_dev.shape[0])
+    dos = torch.empty(ne, dtype=torch.float64, device=freq_dev.device)
+    nd = torch.empty_like(dos)
+    ldfunc = func_dev.shape[1] if func_dev is not None else nb
+    rc = _lib().pp_dos_triangulation_device(_ptr(freq_dev), ldf, nk, nb, _ptr(func_dev), ldfunc, _ptr(tri_dev),
+                                            int(tri_dev.shape[0]), _ptr(energy_dev), ne, _ptr(dos), _ptr(nd),
+                                            ctypes.c_void_p(int(stream)))
+    if rc != 0:
+        raise api.PPError(rc, "pp_dos_triangulation_device")
+    return dos, nd
+
+
+def smearing_dos_device(freq_dev, weights_dev, energy_dev, width, natom, method="gaussian", nbands=None, stream=0):
+    import torch
+    nq, ldf = freq_dev.shape
+    nb = ldf if nbands is None else int(nbands)
+    ne = int(energy_dev.shape[0])
+    out = torch.empty(ne, dtype=torch.float64, device=freq_dev.device)
+    m = {"gaussian": 1, "lorentzian": 2}[method]
+    rc = _lib().pp_dos_smearing_device(m, _ptr(freq_dev), ldf, nq, nb, _ptr(weights_dev), float(width),
+                                       _ptr(energy_dev), ne, int(natom), _ptr(out), ctypes.c_void_p(int(stream)))
+    if rc != 0:
+        raise api.PPError(rc, "pp_dos_smearing_device")
+    return out
+
+
+def velocity_weights_device(vel_dev, a=-1, b=-1, nbands=None, stream=0):
+    """Transport-DOS weights v_a v_b (or |v|^2 with a = b = -1) per (q, mode)
+    from a (nq, n, 3) velocity tensor of PhononContext.solve_device."""
+    import torch
+    nq, n, _ = vel_dev.shape
+    nb = n if nbands is None else int(nbands)
+    func = torch.empty((nq, nb), dtype=torch.float64, device=vel_dev.device)
+    rc = _lib().pp_velocity_weights_device(_ptr(vel_dev), 3 * n, nq, nb, int(a), int(b), _ptr(func), nb,
+                                           ctypes.c_void_p(int(stream)))
+    if rc != 0:
+        raise api.PPError(rc, "pp_velocity_weights_device")
+    return func

@@ -104,3 +104,42 @@ def test_grad_phi_vs_fp64_oracle(setup):
         Gref += np.real(M.T * Pu)
     scale = np.abs(Gref).max()
     assert np.abs(G - Gref).max() <= 1e-8 * scale, np.abs(G - Gref).max() / scale
+
+
+def test_grad_q_vs_cd_velocities_n148():
+    """dL/dq at N = 148 (device tensors end to end) against the
+    central-difference group velocities of the library: for L = sum g_j w_j,
+    dL/dq = sum_j g_j dw_j/dq with dw_j/dk the CD velocity over the
+    reference's unit factor; g is constant over degenerate clusters (where
+    only the cluster sums are basis independent)."""
+    import torch
+    from parphom_gb300.autograd import PhononSpectrum, C_OMEGA, VEL_FACTOR, cluster_mean
+    c = synth.tblg_cell(3)
+    phi = synth.spring_force_constants(c, seed=0)
+    dev = torch.device("cuda", 0)
+    spec = PhononSpectrum.from_cell(c, precision=api.PP_PREC_MIXED, batch=4)
+    qs = synth.random_qpoints(5, seed=17)
+    q = torch.tensor(qs, device=dev, requires_grad=True)
+    pt = torch.tensor(phi, device=dev)
+    w = spec.frequencies(q, pt)
+    assert w.is_cuda
+    lam = torch.sign(w.detach()) * (w.detach() / C_OMEGA) ** 2
+    g = cluster_mean(lam, torch.linspace(-1.0, 1.0, w.shape[1], device=dev, dtype=torch.float64).expand_as(w))
+    (g * w).sum().backward()
+    assert q.grad.is_cuda
+    with api.PhononContext.from_cell(c, phi) as ctx:
+        r = ctx.solve(qs, api.EigOpts(jobz="N", vel=True, vel_method="C", precision=api.PP_PREC_FP64),
+                      want_z=False)
+    a = np.abs(r.w)
+    dwdk = r.vel * (C_OMEGA ** 2 / VEL_FACTOR) * (np.maximum(2 * a, 1e-3) / np.maximum(2 * a, 1e-300))[..., None]
+    dwdq = dwdk @ spec.rec_lat.T
+    expect = np.einsum("tn,tnk->tk", g.cpu().numpy(), dwdq)
+    got = q.grad.cpu().numpy()
+    scale = np.abs(expect).max()
+    assert np.abs(got - expect).max() <= 1e-6 * scale, np.abs(got - expect).max() / scale
+    # a second forward with changed force constants reuses the context
+    h = spec._ctx._h.value
+    w2 = spec.frequencies(q.detach(), pt * 1.01)
+    assert spec._ctx._h.value == h
+    np.testing.assert_allclose(w2.cpu().numpy(), w.detach().cpu().numpy() * np.sqrt(1.01), rtol=1e-9)
+    spec.close()

@@ -188,3 +188,45 @@ def test_uneven_cells_one_batch(tblg28, cell148, prec):
                 ov = np.abs(np.einsum("ij,ij->j", Z.conj(), Zs))
                 assert np.abs(ov - 1).max() < 1e-9
     ctx364.close()
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_error_estimates(cell148, prec):
+    """Per-eigenpair error estimates (want_resid): the residual equals an
+    independent FP64 residual of the returned pair, the frequency bound covers
+    the difference to the oracle, and the eigenvector bound covers the angle
+    to the oracle's eigenvector for well-separated modes."""
+    S, ctx = cell148
+    qs = synth.random_qpoints(2, seed=21)
+    res = ctx.solve(qs, api.EigOpts(jobz="V", vel=True, want_resid=True, precision=prec))
+    fast = ctx.solve(qs, api.EigOpts(jobz="N", vel=True, want_resid=True, precision=prec), want_z=False)
+    n = S.n
+    eps = np.finfo(float).eps
+    cw = O.C1 * O.C2
+    for t, q in enumerate(qs):
+        ref = O.solve_q(S, q, jobz="V")
+        D = S.dynmat(q)
+        lam_ref = ref["lam"]
+        Dn = np.abs(lam_ref).max()
+        w, z = res.w[t, :n], res.z[t][:, :n]
+        lam = np.sign(w) * (w / cw) ** 2
+        # the estimates do not depend on whether eigenvectors are returned
+        np.testing.assert_allclose(fast.werr[t, :n], res.werr[t, :n], rtol=1e-6, atol=1e-30)
+        r_np = np.linalg.norm(D @ z - z * lam[None, :], axis=0)
+        assert np.all(np.abs(res.resid[t, :n] - r_np) <= 0.2 * r_np + 1e-14 * Dn), \
+            np.abs(res.resid[t, :n] - r_np).max()
+        assert res.resid[t, :n].max() <= 1e-11 * Dn
+        # frequency bound vs the oracle (its own error: a few n eps ||D|| in lambda)
+        big = np.abs(ref["w_cm"]) >= 1.0
+        dlo = 4 * n * eps * Dn
+        oracle_w = cw * dlo / (2 * np.sqrt(np.abs(lam_ref)))
+        dw = np.abs(w - ref["w_cm"])
+        assert np.all((dw <= res.werr[t, :n] + oracle_w)[big])
+        assert res.werr[t, :n][big].max() <= 1e-4
+        # eigenvector bound on well-separated modes
+        gaps = np.minimum(np.diff(lam_ref, prepend=-np.inf), np.diff(lam_ref, append=np.inf))
+        sep = gaps > 1e-6 * Dn
+        ov = np.abs(np.einsum("ij,ij->j", z.conj(), ref["z"]))
+        sin = np.sqrt(np.maximum(0.0, 1.0 - ov ** 2))
+        oracle_z = 4 * n * eps * Dn / gaps
+        assert np.all((sin <= res.zerr[t, :n] + oracle_z + 1e-7)[sep])
