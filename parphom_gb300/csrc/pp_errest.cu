@@ -2,8 +2,9 @@
 //
 // For eigenpair j of D(q) (lambda_j from the bisection, z_j the library's
 // eigenvector, in either precision form) with D assembled again in FP64:
-//   s1 = ||D z - lambda z||^2,  s2 = Re z^H D z,  s3 = ||z||^2
-//   rho = s2 / s3 (Rayleigh quotient),  t = rho - lambda
+//   r = D z - lambda z,  s1 = ||r||^2,  s2 = Re z^H r,  s3 = ||z||^2
+//   t = s2 / s3 = rho - lambda  (rho the Rayleigh quotient; taken from the
+//   small residual, not as z^H D z - lambda, so it carries no cancellation)
 //   ||D z - rho z||^2 = s1 - t^2 s3          (D z - rho z is orthogonal to z)
 //   gap = distance from lambda_j to the nearest other computed eigenvalue
 // and reports
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(256) k_resid(const z64 *Db, int64_t ldd, int64
           const z64 z = ld_vec<EFMT>(E, b * sE + r + lde * c);
           const double xr = acc[p][q].re - lam * z.re, xi = acc[p][q].im - lam * z.im;
           s1 += xr * xr + xi * xi;
-          s2 += z.re * acc[p][q].re + z.im * acc[p][q].im;
+          s2 += z.re * xr + z.im * xi;
           s3 += z.re * z.re + z.im * z.im;
         }
       }
@@ -145,7 +146,7 @@ __global__ void k_errfin(const double *sums, int64_t mstride, const double *ww, 
   if (j + 1 < m) gap = fmin(gap, w[j + 1] - lam);
   gap = fmax(gap, 1e-300);
   const double res = sqrt(s1 / s3);
-  const double t = s2 / s3 - lam;
+  const double t = s2 / s3;
   const double rr = fmax(s1 - t * t * s3, 0.0) / s3;  // ||D z - rho z||^2 / ||z||^2
   const double dlam = fmin(res, fabs(t) + rr / gap);
   double we = dlam;
