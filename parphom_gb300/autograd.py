@@ -57,7 +57,8 @@ class PhononSpectrum:
         self.keep_vectors = keep_vectors
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self._ctx = None
-        self._phi_key = None
+        self._phi = None        # the tensor last uploaded (kept alive: its address cannot be reused)
+        self._phi_ver = None    # its (address, version, layout) key
 
     @classmethod
     def from_cell(cls, cell, **kw):
@@ -67,8 +68,10 @@ class PhononSpectrum:
         """The cell's context with `phi` as its force constants: created on
         the first call, Phi replaced on the device afterwards (skipped when
         the same tensor, unchanged, was uploaded last)."""
-        key = (phi.data_ptr(), phi._version, phi.device)
-        if self._ctx is not None and key == self._phi_key:
+        # same storage, layout and version as the tensor uploaded last (which is
+        # kept alive, so no other tensor can have taken its address)
+        key = (phi.data_ptr(), phi._version, tuple(phi.shape), tuple(phi.stride()), phi.device, phi.dtype)
+        if self._ctx is not None and key == self._phi_ver:
             return self._ctx
         if self._ctx is None:
             fc = phi.detach().to(torch.float64).cpu().numpy()
@@ -78,13 +81,14 @@ class PhononSpectrum:
             fcd = phi.detach().to(device=self.device, dtype=torch.float64).T.contiguous()
             torch.cuda.current_stream(self.device).synchronize()
             self._ctx.update_fc_device(fcd.data_ptr(), self.n)
-        self._phi_key = key
+        self._phi, self._phi_ver = phi, key
         return self._ctx
 
     def close(self):
         if self._ctx is not None:
             self._ctx.close()
             self._ctx = None
+        self._phi = None
 
     def frequencies(self, q: torch.Tensor, phi: torch.Tensor) -> torch.Tensor:
         return _Spectrum.apply(q, phi, self)

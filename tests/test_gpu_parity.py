@@ -228,7 +228,10 @@ def test_error_estimates(cell148, prec):
         # eigenvector bound on well-separated modes
         gaps = np.minimum(np.diff(lam_ref, prepend=-np.inf), np.diff(lam_ref, append=np.inf))
         sep = gaps > 1e-6 * Dn
-        ov = np.abs(np.einsum("ij,ij->j", z.conj(), ref["z"]))
-        sin = np.sqrt(np.maximum(0.0, 1.0 - ov ** 2))
+        # sin(angle) as the norm of the part of z orthogonal to the oracle's
+        # vector (no cancellation, unlike sqrt(1 - |z^H z_ref|^2))
+        zh = z / np.linalg.norm(z, axis=0)[None, :]
+        proj = ref["z"] * np.einsum("ij,ij->j", ref["z"].conj(), zh)[None, :]
+        sin = np.linalg.norm(zh - proj, axis=0)
         oracle_z = 4 * n * eps * Dn / gaps
         assert np.all((sin <= res.zerr[t, :n] + oracle_z + 1e-7)[sep])
