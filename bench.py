@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi (profiler runs)")
     p.add_argument("--roofline-kernels", default="assemble,colupd,refl,hemv,dots,wcorr,wfin,her2k,bisect,invit,vhx,btred,applyV,vel,xhz")
+    p.add_argument("--no-configs", action="store_true", help="skip the samples of the other configurations")
     p.add_argument("--large-cell", type=int, default=0, metavar="NQ",
                    help="instead of the headline bench: NQ q-points around K of the N=11164 cell, range I 1..256 "
                         "with eigenvectors and velocities, with residual and orthogonality checks")
@@ -323,6 +324,8 @@ def main():
         dom = max(ktimes, key=lambda k: ktimes[k][1])
         roof = roofline_for(dom, ktimes[dom], n, B * args.steps)
         roof["kernel_ms_share"] = {k: round(v[1] / sum(x[1] for x in ktimes.values()), 4) for k, v in ktimes.items()}
+    if rank == 0 and not args.no_configs:
+        extra["configs"] = other_configs(dev)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, ref = cpu_baseline(cell, phi, q_all)
@@ -383,6 +386,133 @@ def roofline_for(kclass, rec, n, nq):
     ach = flops / (ms / 1e3) / 1e12
     return {"bound": "fp32-simt (double-float)", "kernel": kclass, "achieved": ach, "peak": None, "unit": "TFLOP/s",
             "frac": None, "launches": launches, "avg_launch_ms": ms / launches}
+
+
+ALL_KERNELS = "assemble,colupd,refl,hemv,dots,wcorr,wfin,her2k,bisect,invit,vhx,btred,applyV,vel,xhz"
+
+
+def timed(fn, nq, n, kclasses=ALL_KERNELS):
+    """q-points/s of one call of fn through the host C ABI (host buffers in and
+    out, copies included), then the same call again with per-kernel events
+    for the roofline of its dominant kernel class."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    from parphom_gb300 import api
+    api.kernel_timer(kclasses)
+    fn()
+    torch.cuda.synchronize()
+    kt = api.kernel_timer_report()
+    api.kernel_timer("")
+    roof = None
+    if kt:
+        dom = max(kt, key=lambda k: kt[k][1])
+        roof = roofline_for(dom, kt[dom], n, nq)
+        roof = {k: roof.get(k) for k in ("kernel", "bound", "achieved", "unit", "frac", "peak")}
+        roof["share_of_kernel_time"] = round(kt[dom][1] / sum(v[1] for v in kt.values()), 3)
+    return out, {"value": nq / dt, "unit": UNIT, "s": dt, "n_q": nq, "roofline": roof}
+
+
+def oracle_check(S, q, w, vel, m=None):
+    """Largest frequency difference (|w| >= 1 cm^-1) and per-mode velocity
+    difference of one q-point against the oracle."""
+    from oracle import oracle as O
+    ref = O.solve_q(S, q, vel=vel is not None, vel_method="A")
+    k = len(ref["w_cm"]) if m is None else m
+    big = np.abs(ref["w_cm"]) >= 1.0
+    out = {"q": list(map(float, q)), "max_abs_dw_cm1": float(np.abs(w[:k] - ref["w_cm"])[big].max())}
+    if vel is not None:
+        out["max_dv_rel_per_mode"] = per_mode_dv(vel[:k], ref["vel"], ref["lam"], float(np.abs(ref["vel"]).max()))
+    return out
+
+
+def other_configs(dev):
+    """Short samples of the other configurations of the workload list (each
+    q-points/s through the host C ABI, the dominant kernel's roofline, and
+    accuracy on one q-point against the oracle or the FP64 form).  Sample
+    sizes are stated per entry; the full q sets are the parity tests' and the
+    README's business."""
+    import torch
+    from oracle import oracle as O
+    from parphom_gb300 import api, autograd, synth
+    res = {}
+    # 1: N=148, FP64, 64 q on Gamma-K-M-Gamma, range A, eigenvalues only
+    c = synth.tblg_cell(3)
+    phi = synth.spring_force_constants(c, seed=0)
+    S = O.System.from_cell(c, phi)
+    with api.PhononContext.from_cell(c, phi) as ctx:
+        q = synth.band_path(64)
+        o = api.EigOpts(jobz="N", precision=api.PP_PREC_FP64)
+        ctx.solve(q[:8], o)
+        r, e = timed(lambda: ctx.solve(q, o, want_z=False), 64, c.n)
+        e.update({"workload": "N=148 (3N=444), FP64, 64 q band path, range A, no vectors", "sample": "all 64 q",
+                  "vs_oracle": oracle_check(S, q[5], r.w[5], None)})
+        res["1_n148_fp64"] = e
+    # 2: N=868, band path, vectors + analytic v_g, FP64 form and mixed form
+    c = synth.tblg_cell(8)
+    phi = synth.spring_force_constants(c, seed=0)
+    S = O.System.from_cell(c, phi)
+    with api.PhononContext.from_cell(c, phi) as ctx:
+        q = synth.band_path(256)[::8]   # 32 of the 256
+        ent = {"workload": "N=868 (3N=2604), band path, eigenvectors + analytic v_g",
+               "sample": "32 of the 256 band-path q (every 8th)"}
+        outs = {}
+        for name, prec in (("fp64", api.PP_PREC_FP64), ("mixed", api.PP_PREC_MIXED)):
+            o = api.EigOpts(jobz="V", vel=True, precision=prec)
+            ctx.solve(q[:2], o)
+            outs[name], ent[name] = timed(lambda: ctx.solve(q, o), len(q), c.n)
+        ent["mixed_over_fp64"] = ent["mixed"]["value"] / ent["fp64"]["value"]
+        big = np.abs(outs["fp64"].w) >= 1.0
+        ent["mixed_vs_fp64"] = {
+            "max_abs_dw_cm1": float(np.abs(outs["fp64"].w - outs["mixed"].w)[big].max()),
+            "max_dv_rel_per_mode": max(per_mode_dv(outs["mixed"].vel[t], outs["fp64"].vel[t],
+                                                   w_to_lambda(outs["fp64"].w[t]),
+                                                   float(np.abs(outs["fp64"].vel).max())) for t in range(len(q)))}
+        ent["vs_oracle"] = oracle_check(S, q[3], outs["mixed"].w[3], outs["mixed"].vel[3])
+        res["2_n868_vectors_velocities"] = ent
+    # 3: uneven cells in shared batches (pp_solve_multi), eigenvalues + velocities
+    cells = [synth.tblg_cell(m) for m in (3, 5, 8)]
+    ctxs = [api.PhononContext.from_cell(cc, synth.spring_force_constants(cc, seed=0)) for cc in cells]
+    try:
+        g = synth.uniform_grid(8)
+        q = np.vstack([g, g, g])
+        cell_of = np.repeat(np.arange(3), len(g))
+        o = api.EigOpts(jobz="N", vel=True, precision=api.PP_PREC_MIXED)
+        api.solve_multi(ctxs, cell_of[:6], q[:6], o, want_z=False)
+        r, e = timed(lambda: api.solve_multi(ctxs, cell_of, q, o, want_z=False), len(q), cells[2].n)
+        e.update({"workload": "N=148/364/868 in shared batches, Gamma-centred grids, w + v_g, mixed",
+                  "sample": "8x8 grid per cell (64 q each, 192 q) of the 32x32 grids"})
+        res["3_uneven_cells"] = e
+    finally:
+        for cc in ctxs:
+            cc.close()
+    # 4: forward + backward (dL/dq, dL/dPhi) at N=1588
+    c = synth.tblg_cell(11)
+    phi = synth.spring_force_constants(c, seed=0)
+    rng = np.random.default_rng(1)
+    spec = autograd.PhononSpectrum.from_cell(c, precision=api.PP_PREC_MIXED, batch=8)
+    try:
+        q = torch.tensor(synth.band_path(128)[::16], device=dev, requires_grad=True)   # 8 of the 128
+        pt = torch.tensor(phi, device=dev, requires_grad=True)
+        target = spec.frequencies(q.detach(), pt.detach()) * torch.tensor(
+            1.0 + 0.03 * rng.uniform(-1, 1, (len(q), c.n)), device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w = spec.frequencies(q, pt)
+        loss = ((w - target) ** 2).sum()
+        loss.backward()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        res["4_n1588_forward_backward"] = {
+            "workload": "N=1588, loss = sum (w - w_target)^2, dL/dq and dL/dPhi (autograd.Function, device tensors)",
+            "sample": "8 of the 128 q", "value": len(q) / dt, "unit": "q-pts/s (forward + backward)", "s": dt,
+            "grad_phi_symmetric": bool(torch.allclose(pt.grad, pt.grad.T))}
+    finally:
+        spec.close()
+    return res
 
 
 def cpu_baseline(cell, phi, q_all):
