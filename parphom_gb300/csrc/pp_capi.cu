@@ -46,7 +46,8 @@ int device_sms() {
 
 unsigned kt_mask = 0;
 static const char *kt_names[KT_N] = {"assemble", "colupd", "refl", "hemv", "dots", "wcorr", "wfin", "her2k",
-                                     "bisect", "invit", "vhx", "btred", "applyV", "vel", "xhz"};
+                                     "bisect", "invit", "vhx", "btred", "applyV", "vel", "xhz", "bandqr", "bandmv",
+                                     "bulge", "q2"};
 struct KtPending {
   int k;
   cudaEvent_t a, b;
@@ -209,6 +210,19 @@ void free_ws(pp_ctx *c) {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// The two-stage reduction needs at least three panels.
+bool band_possible(int64_t n) { return n >= 128; }
+
+// Mixed form: two-stage reduction (dense -> band -> tridiagonal) instead of
+// the one-stage one.  PARPHOM_GPU_BAND=1 / 0 forces it on / off.
+bool band_wanted(int64_t n) {
+  if (!band_possible(n)) return false;
+  const char *e = getenv("PARPHOM_GPU_BAND");
+  if (e && e[0] == '1') return true;
+  if (e && e[0] == '0') return false;
+  return false;
+}
+
 // Carve every batch buffer out of one allocation.
 int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int64_t nbr_max) {
   if (c->ws && B <= c->cap_B && mcap <= c->cap_m && n == c->cap_n && nbnd_max <= c->cap_nbnd &&
@@ -280,6 +294,19 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   add((void **)&w.tcS, (size_t)B * w.sTcS);
   add((void **)&w.tcE, 4 * (size_t)B * w.sTcE);
   add((void **)&w.tcErr, 4 * (size_t)B);
+  // two-stage reduction (mixed form)
+  if (band_possible(n)) {
+    w.nyp = (int)((n + 255) / 256);
+    w.nq2 = q2_count(n);
+    add(&w.Vb, 16 * (size_t)B * lda * 32);
+    add(&w.Ub, 16 * (size_t)B * lda * 32);
+    add(&w.Xb, 16 * (size_t)B * lda * 32);
+    add((void **)&w.Yp, 16 * (size_t)B * w.nyp * 1024);
+    add((void **)&w.Mb, 16 * (size_t)B * 1024);
+    add(&w.AB, 16 * (size_t)B * 64 * n);
+    add(&w.q2v, 16 * (size_t)B * w.nq2 * 32);
+    add((void **)&w.q2t, 16 * (size_t)B * w.nq2);
+  }
   add((void **)&c->vpart, 8 * (size_t)B * c->nsplit * 3 * mcap + 16 * (size_t)B * nbnd * 3);
   add((void **)&c->vraw, 8 * (size_t)B * 3 * mcap);
   add((void **)&c->d_q, 8 * (size_t)B * 3);
@@ -298,6 +325,7 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   for (auto &p : parts) *p.first = (char *)base + p.second;
   // opt the tensor-core kernel into its shared memory (outside any capture)
   TRY_CUDA(prepare_her2k_tc());
+  if (band_possible(n)) TRY_CUDA(prepare_band());
   c->ws = base;
   c->ws_bytes = off;
   w.bytes = off;
@@ -319,6 +347,9 @@ size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd, int64_t nbr) 
                16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
                16 * (size_t)((n + 63) / 64) * 32 * 32 + her2k_tc_bytes(n) + 8 * (size_t)(n + 128) +
                8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd + 16 * (size_t)nbr * (n + mcap);
+  if (band_possible(n))
+    per += 16 * (size_t)n * 32 * 3 + 16 * (size_t)((n + 255) / 256 + 1) * 1024 + 16 * (size_t)64 * n +
+           16 * (size_t)q2_count(n) * 33;
   return per * B;
 }
 
@@ -372,6 +403,16 @@ EigWork view_of(const EigWork &w, int off, int cnt) {
   v.Wp = sh(w.Wp, 16 * (size_t)w.ksplit * 32 * w.ldwp);
   v.Xr = sh(w.Xr, 16 * (size_t)w.lda * std::max(w.nbr, 1));
   v.Eb = sh(w.Eb, 16 * (size_t)std::max(w.nbr, 1) * w.mcap);
+  if (w.q2v) {
+    v.Vb = sh(w.Vb, 16 * (size_t)w.lda * 32);
+    v.Ub = sh(w.Ub, 16 * (size_t)w.lda * 32);
+    v.Xb = sh(w.Xb, 16 * (size_t)w.lda * 32);
+    v.Yp = (z64 *)sh(w.Yp, 16 * (size_t)w.nyp * 1024);
+    v.Mb = (z64 *)sh(w.Mb, 16 * 1024);
+    v.AB = sh(w.AB, 16 * (size_t)64 * w.nmax);
+    v.q2v = sh(w.q2v, 16 * (size_t)w.nq2 * 32);
+    v.q2t = (z64 *)sh(w.q2t, 16 * (size_t)w.nq2);
+  }
   if (w.tcS) {
     v.tcS = (uint8_t *)sh(w.tcS, (size_t)w.sTcS);
     v.tcE = (int *)sh(w.tcE, 4 * (size_t)w.sTcE);
@@ -395,10 +436,16 @@ bool rows_only_mode(const Geometry &g, const pp_eig_opts *o, bool want_z) {
 int eig_stages(pp_ctx *c, EigWork &w, const pp_eig_opts *o, bool want_z, cudaStream_t s) {
   const int prec = o->precision;
   const bool vecs = needs_vectors(o);
-  if (prec == PP_PREC_MIXED)
+  w.voff = 1;
+  w.band = 0;
+  if (prec == PP_PREC_MIXED && w.q2v && band_wanted(w.nmax)) {
+    TRY_CUDA(band_reduce(w, s));
+    TRY_CUDA(band_to_tridiag(w, s));
+  } else if (prec == PP_PREC_MIXED) {
     TRY_CUDA(tridiagonalize<df>(w, s));
-  else
+  } else {
     TRY_CUDA(tridiagonalize<double>(w, s));
+  }
   TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s,
                                prec == PP_PREC_MIXED));
   if (vecs) {
@@ -499,7 +546,7 @@ int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_
   char key[160];
   snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d|%d|%d", c->ws, B, o->precision,
            o->jobz, o->range, o->vel_method, o->vel, (long long)o->il, (long long)o->iu, o->vl, o->vu, o->abstol,
-           want_z ? 1 : 0, split_ways(), o->want_resid ? 1 : 0);
+           want_z ? 1 : 0, split_ways(), (o->want_resid ? 1 : 0) | (band_wanted(c->w.nmax) ? 2 : 0));
   cudaStream_t s = c->stream;
   if (c->gexec && strcmp(key, c->gkey) == 0) {
     TRY_CUDA(cudaGraphLaunch(c->gexec, s));
