@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi (profiler runs)")
-    p.add_argument("--roofline-kernels", default="assemble,colupd,refl,hemv,dots,wcorr,wfin,her2k,bisect,invit,vhx,btred,applyV,vel,xhz,bandqr,bandmv,bulge,q2")
+    p.add_argument("--roofline-kernels", default="assemble,colupd,refl,hemv,dots,wcorr,wfin,her2k,bisect,invit,vhx,btred,applyV,vel,xhz")
     p.add_argument("--no-configs", action="store_true", help="skip the samples of the other configurations")
     p.add_argument("--large-cell", type=int, default=0, metavar="NQ",
                    help="instead of the headline bench: NQ q-points around K of the N=11164 cell, range I 1..256 "
@@ -336,7 +336,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "df32x2 (double-float), f64 tridiagonal",
                 "data": "synthetic",
                 "config": {"workload": WORKLOAD, "q_per_step_per_gpu": B, "precision": "mixed",
-                           "l2": "inputs larger than L2 (363 MB matrix per q)", "parallelism": f"replicas x{world}"},
+                           "l2": "inputs larger than L2 (363 MB matrix per q)", "parallelism": f"replicas x{world}",
+                           "autotuned": api.autotune_report()},
                 "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "roofline": roof,
                 "cpu_baseline": cpu}
         line.update(extra)

@@ -291,6 +291,14 @@ PP_API int pp_heevx_values_noalloc(double *a_dev, int64_t lda, int64_t n, char r
 PP_API int pp_ktimer_enable(const char *names);
 PP_API int pp_ktimer_report(char *buf, int64_t len);
 
+/* The launch configurations the autotuner chose in this process, one line
+ * per (device, order, batch size, options): the number of streams a batch
+ * is split over and the persistent blocks per SM of the Hermitian mat-vec,
+ * with the batch's GPU time.  The first solve of each combination times the
+ * candidates on its own first batch (PARPHOM_GPU_TUNE=0 or an explicit
+ * PARPHOM_GPU_SPLIT turns this off).  No counterpart in the reference. */
+PP_API int pp_autotune_report(char *buf, int64_t len);
+
 /* Test hook for the bounded device waits (no counterpart in the reference).
  * Arms a one-shot stall: the next mixed-form tensor-core trailing update
  * whose batch contains batch matrix `matrix` (0-based index within one

@@ -35,7 +35,7 @@ EXPORTED = ("pp_ctx_create", "pp_ctx_destroy", "pp_solve_batch", "pp_solve_batch
             "pp_strerror", "pp_version", "pp_kernel_launches", "pp_ktimer_enable", "pp_ktimer_report",
             "pp_heevx_values_noalloc", "pp_backward_phi", "pp_solve_multi", "pp_debug_stall_tc_wait",
             "pp_ctx_update_fc", "pp_dos_triangulation_device", "pp_dos_smearing_device",
-            "pp_velocity_weights_device")
+            "pp_velocity_weights_device", "pp_autotune_report")
 PP_ERR_SIZE = 1008
 PP_NOALLOC_MAX_N = 1536
 
@@ -114,6 +114,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.pp_backward_phi.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _i64, ctypes.c_void_p, _i64, _i64, _i64,
                                   ctypes.c_void_p, _i64, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
     L.pp_backward_phi.restype = ctypes.c_int
+    L.pp_autotune_report.argtypes = [ctypes.c_char_p, _i64]
+    L.pp_autotune_report.restype = ctypes.c_int
     L.pp_debug_stall_tc_wait.argtypes = [_i64, _i64]
     L.pp_debug_stall_tc_wait.restype = ctypes.c_int
     L.pp_ktimer_enable.argtypes = [ctypes.c_char_p]
@@ -377,6 +379,14 @@ def debug_stall_tc_wait(matrix: int, cycles: int) -> None:
     rc = load().pp_debug_stall_tc_wait(int(matrix), int(cycles))
     if rc != 0:
         raise PPError(rc, "pp_debug_stall_tc_wait")
+
+
+def autotune_report() -> list:
+    """The autotuner's choices so far, one string per tuned combination."""
+    L = load()
+    buf = ctypes.create_string_buffer(8192)
+    L.pp_autotune_report(buf, 8192)
+    return [x for x in buf.value.decode().splitlines() if x]
 
 
 def kernel_launches() -> int:

@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, "libparphom_gpu.so")
 HOST = os.path.join(HERE, "host")
 EXE = os.path.join(LIBDIR, "parphom_gpu.x")
 HOST_SOURCES = ["h5min.cpp", "inputs.cpp", "parphom_gpu_main.cpp"]
-SOURCES = ["pp_capi.cu", "pp_dynmat.cu", "pp_eigen.cu", "pp_noalloc.cu", "pp_dos.cu", "pp_tc.cu", "pp_errest.cu", "pp_band.cu"]
+SOURCES = ["pp_capi.cu", "pp_dynmat.cu", "pp_eigen.cu", "pp_noalloc.cu", "pp_dos.cu", "pp_tc.cu", "pp_errest.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
 

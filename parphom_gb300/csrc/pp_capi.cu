@@ -46,8 +46,7 @@ int device_sms() {
 
 unsigned kt_mask = 0;
 static const char *kt_names[KT_N] = {"assemble", "colupd", "refl", "hemv", "dots", "wcorr", "wfin", "her2k",
-                                     "bisect", "invit", "vhx", "btred", "applyV", "vel", "xhz", "bandqr", "bandmv",
-                                     "bulge", "q2"};
+                                     "bisect", "invit", "vhx", "btred", "applyV", "vel", "xhz"};
 struct KtPending {
   int k;
   cudaEvent_t a, b;
@@ -122,9 +121,11 @@ struct pp_ctx {
   static constexpr int MAX_SPLIT = 16;
   cudaStream_t aux[MAX_SPLIT - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[MAX_SPLIT - 1] = {};
+  // launch configuration of the current batch (autotuned or from the switches)
+  int cur_split = 8, cur_bps = 6;
   // captured CUDA graph of the last batch configuration
   cudaGraphExec_t gexec = nullptr;
-  char gkey[160] = {0};
+  char gkey[192] = {0};
   int64_t glaunches = 0;  // kernels in the captured graph
 };
 
@@ -210,19 +211,6 @@ void free_ws(pp_ctx *c) {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// The two-stage reduction needs at least three panels.
-bool band_possible(int64_t n) { return n >= 128; }
-
-// Mixed form: two-stage reduction (dense -> band -> tridiagonal) instead of
-// the one-stage one.  PARPHOM_GPU_BAND=1 / 0 forces it on / off.
-bool band_wanted(int64_t n) {
-  if (!band_possible(n)) return false;
-  const char *e = getenv("PARPHOM_GPU_BAND");
-  if (e && e[0] == '1') return true;
-  if (e && e[0] == '0') return false;
-  return false;
-}
-
 // Carve every batch buffer out of one allocation.
 int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int64_t nbr_max) {
   if (c->ws && B <= c->cap_B && mcap <= c->cap_m && n == c->cap_n && nbnd_max <= c->cap_nbnd &&
@@ -294,19 +282,6 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   add((void **)&w.tcS, (size_t)B * w.sTcS);
   add((void **)&w.tcE, 4 * (size_t)B * w.sTcE);
   add((void **)&w.tcErr, 4 * (size_t)B);
-  // two-stage reduction (mixed form)
-  if (band_possible(n)) {
-    w.nyp = (int)((n + 255) / 256);
-    w.nq2 = q2_count(n);
-    add(&w.Vb, 16 * (size_t)B * lda * 32);
-    add(&w.Ub, 16 * (size_t)B * lda * 32);
-    add(&w.Xb, 16 * (size_t)B * lda * 32);
-    add((void **)&w.Yp, 16 * (size_t)B * w.nyp * 1024);
-    add((void **)&w.Mb, 16 * (size_t)B * 1024);
-    add(&w.AB, 16 * (size_t)B * 64 * n);
-    add(&w.q2v, 16 * (size_t)B * w.nq2 * 32);
-    add((void **)&w.q2t, 16 * (size_t)B * w.nq2);
-  }
   add((void **)&c->vpart, 8 * (size_t)B * c->nsplit * 3 * mcap + 16 * (size_t)B * nbnd * 3);
   add((void **)&c->vraw, 8 * (size_t)B * 3 * mcap);
   add((void **)&c->d_q, 8 * (size_t)B * 3);
@@ -325,7 +300,6 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   for (auto &p : parts) *p.first = (char *)base + p.second;
   // opt the tensor-core kernel into its shared memory (outside any capture)
   TRY_CUDA(prepare_her2k_tc());
-  if (band_possible(n)) TRY_CUDA(prepare_band());
   c->ws = base;
   c->ws_bytes = off;
   w.bytes = off;
@@ -347,9 +321,6 @@ size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd, int64_t nbr) 
                16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
                16 * (size_t)((n + 63) / 64) * 32 * 32 + her2k_tc_bytes(n) + 8 * (size_t)(n + 128) +
                8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd + 16 * (size_t)nbr * (n + mcap);
-  if (band_possible(n))
-    per += 16 * (size_t)n * 32 * 3 + 16 * (size_t)((n + 255) / 256 + 1) * 1024 + 16 * (size_t)64 * n +
-           16 * (size_t)q2_count(n) * 33;
   return per * B;
 }
 
@@ -403,16 +374,6 @@ EigWork view_of(const EigWork &w, int off, int cnt) {
   v.Wp = sh(w.Wp, 16 * (size_t)w.ksplit * 32 * w.ldwp);
   v.Xr = sh(w.Xr, 16 * (size_t)w.lda * std::max(w.nbr, 1));
   v.Eb = sh(w.Eb, 16 * (size_t)std::max(w.nbr, 1) * w.mcap);
-  if (w.q2v) {
-    v.Vb = sh(w.Vb, 16 * (size_t)w.lda * 32);
-    v.Ub = sh(w.Ub, 16 * (size_t)w.lda * 32);
-    v.Xb = sh(w.Xb, 16 * (size_t)w.lda * 32);
-    v.Yp = (z64 *)sh(w.Yp, 16 * (size_t)w.nyp * 1024);
-    v.Mb = (z64 *)sh(w.Mb, 16 * 1024);
-    v.AB = sh(w.AB, 16 * (size_t)64 * w.nmax);
-    v.q2v = sh(w.q2v, 16 * (size_t)w.nq2 * 32);
-    v.q2t = (z64 *)sh(w.q2t, 16 * (size_t)w.nq2);
-  }
   if (w.tcS) {
     v.tcS = (uint8_t *)sh(w.tcS, (size_t)w.sTcS);
     v.tcE = (int *)sh(w.tcE, 4 * (size_t)w.sTcE);
@@ -436,16 +397,10 @@ bool rows_only_mode(const Geometry &g, const pp_eig_opts *o, bool want_z) {
 int eig_stages(pp_ctx *c, EigWork &w, const pp_eig_opts *o, bool want_z, cudaStream_t s) {
   const int prec = o->precision;
   const bool vecs = needs_vectors(o);
-  w.voff = 1;
-  w.band = 0;
-  if (prec == PP_PREC_MIXED && w.q2v && band_wanted(w.nmax)) {
-    TRY_CUDA(band_reduce(w, s));
-    TRY_CUDA(band_to_tridiag(w, s));
-  } else if (prec == PP_PREC_MIXED) {
+  if (prec == PP_PREC_MIXED)
     TRY_CUDA(tridiagonalize<df>(w, s));
-  } else {
+  else
     TRY_CUDA(tridiagonalize<double>(w, s));
-  }
   TRY_CUDA(tridiag_eigenvalues(w, o->range, o->vl / C_RANGE, o->vu / C_RANGE, o->il, o->iu, o->abstol, s,
                                prec == PP_PREC_MIXED));
   if (vecs) {
@@ -490,7 +445,8 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   const int prec = o->precision;
   TRY_CUDA(assemble_batch(c->g, c->d_q, B, w.A, w.lda, w.sA, prec == PP_PREC_MIXED ? 1 : 0, s));
   (void)mcap;
-  const int ways = pp::kt_mask ? 1 : std::min(B, split_ways());
+  const int ways = pp::kt_mask ? 1 : std::min(B, c->cur_split);
+  w.hemv_bps = c->cur_bps;
   if (ways >= 2) {
     if (!c->ev_fork) TRY_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     for (int k = 0; k < ways - 1; ++k) {
@@ -532,6 +488,36 @@ int run_batch(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   return PP_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner.  The launch configuration of a batch -- how many streams the
+// batch is split over, and how many persistent blocks per SM the Hermitian
+// mat-vec runs with -- is chosen the first time a (device, order, batch size,
+// options) combination is solved: each candidate's captured graph is timed
+// on the GPU (CUDA events around its launch) over the call's own first
+// batch, greedily (split first, then the mat-vec blocks), and the fastest is
+// kept for the process.  PARPHOM_GPU_TUNE=0 or an explicit PARPHOM_GPU_SPLIT
+// turns it off (split from the switch, 6 blocks per SM).
+struct Tuned {
+  int split, bps;
+  float ms;
+};
+std::mutex g_tune_mu;
+std::vector<std::pair<std::string, Tuned>> g_tuned;
+
+bool autotune_enabled() {
+  const char *e = getenv("PARPHOM_GPU_TUNE");
+  if (e && e[0] == '0') return false;
+  const char *sp = getenv("PARPHOM_GPU_SPLIT");
+  return !(sp && sp[0]);
+}
+
+std::string tune_key(const pp_ctx *c, int B, const pp_eig_opts *o, bool want_z) {
+  char key[160];
+  snprintf(key, sizeof(key), "dev%d n=%lld B=%d prec=%d jobz=%c range=%c vel=%d z=%d resid=%d", c->device,
+           (long long)c->w.nmax, B, o->precision, o->jobz, o->range, o->vel, want_z ? 1 : 0, o->want_resid ? 1 : 0);
+  return key;
+}
+
 bool graphs_enabled() {
   const char *e = getenv("PARPHOM_GPU_GRAPHS");
   return !(e && e[0] == '0');
@@ -540,13 +526,85 @@ bool graphs_enabled() {
 // run_batch through a captured CUDA graph: the launch sequence depends only on
 // the batch size, the options and the workspace, so it is captured once and
 // replayed (one graph launch instead of ~6 launches per matrix column).
+int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z);
+
+// Time one launch configuration: capture its graph and time its launch on
+// the stream.  Returns the milliseconds, or a negative value if the graph
+// path is not available.
+float time_config(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z, int split, int bps) {
+  c->cur_split = split;
+  c->cur_bps = bps;
+  cudaStream_t s = c->stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    if (e0) cudaEventDestroy(e0);
+    return -1.f;
+  }
+  float ms = -1.f;
+  // one launch: the capture and instantiation before it are host work (a
+  // small gap on the GPU timeline next to a batch of seconds)
+  cudaEventRecord(e0, s);
+  const int r = run_batch_graph_cfg(c, B, o, mcap, want_z);
+  cudaEventRecord(e1, s);
+  if (r == PP_OK && c->gexec && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
+
 int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
+  c->cur_split = split_ways();
+  c->cur_bps = 6;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    cs = cudaStreamCaptureStatusActive;
+  }
+  if (autotune_enabled() && B >= 2) {
+    const std::string key = tune_key(c, B, o, want_z);
+    Tuned t{-1, 6, 0.f};
+    {
+      std::lock_guard<std::mutex> g(g_tune_mu);
+      for (auto &kv : g_tuned)
+        if (kv.first == key) t = kv.second;
+    }
+    // tune only where candidates can be timed: graphs on, no per-kernel
+    // timing, no caller capture in progress
+    const bool can_tune = graphs_enabled() && !pp::kt_mask && !tc_stall_armed() && cs == cudaStreamCaptureStatusNone;
+    if (t.split < 0 && !can_tune) t = Tuned{split_ways(), 6, 0.f};
+    if (t.split < 0) {
+      // greedy: split over {4, 8, 16} (at most B), then 4 instead of 6 mat-vec blocks per SM
+      Tuned best{std::min(B, 8), 6, 1e30f};
+      for (int sp : {4, 8, 16}) {
+        if (sp > B && sp != 4) continue;
+        const int spc = std::min(sp, B);
+        const float ms = time_config(c, B, o, mcap, want_z, spc, 6);
+        if (ms > 0.f && ms < best.ms) best = Tuned{spc, 6, ms};
+      }
+      if (best.ms < 1e29f) {
+        const float ms = time_config(c, B, o, mcap, want_z, best.split, 4);
+        if (ms > 0.f && ms < best.ms) best = Tuned{best.split, 4, ms};
+      }
+      if (best.ms > 1e29f) best.ms = 0.f;
+      t = best;
+      std::lock_guard<std::mutex> g(g_tune_mu);
+      g_tuned.push_back({key, t});
+    }
+    c->cur_split = t.split;
+    c->cur_bps = t.bps;
+  }
+  return run_batch_graph_cfg(c, B, o, mcap, want_z);
+}
+
+int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
   // (an armed test stall is a one-shot launch parameter: never captured)
   if (!graphs_enabled() || pp::kt_mask || tc_stall_armed()) return run_batch(c, B, o, mcap, want_z);
-  char key[160];
-  snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d|%d|%d", c->ws, B, o->precision,
+  char key[192];
+  snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d|%d|%d|%d", c->ws, B, o->precision,
            o->jobz, o->range, o->vel_method, o->vel, (long long)o->il, (long long)o->iu, o->vl, o->vu, o->abstol,
-           want_z ? 1 : 0, split_ways(), (o->want_resid ? 1 : 0) | (band_wanted(c->w.nmax) ? 2 : 0));
+           want_z ? 1 : 0, c->cur_split, c->cur_bps, o->want_resid ? 1 : 0);
   cudaStream_t s = c->stream;
   if (c->gexec && strcmp(key, c->gkey) == 0) {
     TRY_CUDA(cudaGraphLaunch(c->gexec, s));
@@ -696,6 +754,21 @@ int pp_ktimer_enable(const char *names) {
     pp::kt_ms[k] = 0.0;
   }
   pp::kt_mask = mask;
+  return PP_OK;
+}
+
+int pp_autotune_report(char *buf, int64_t len) {
+  if (!buf || len <= 0) return -1;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  std::string out;
+  char line[256];
+  for (auto &kv : g_tuned) {
+    snprintf(line, sizeof(line), "%s -> split=%d hemv_blocks_per_sm=%d batch_ms=%.3f\n", kv.first.c_str(),
+             kv.second.split, kv.second.bps, kv.second.ms);
+    out += line;
+  }
+  strncpy(buf, out.c_str(), (size_t)len - 1);
+  buf[len - 1] = 0;
   return PP_OK;
 }
 

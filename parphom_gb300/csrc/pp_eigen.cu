@@ -533,8 +533,9 @@ __global__ void __launch_bounds__(256) k_her2k(C<R> *Ab, int64_t lda, int64_t sA
     }
 }
 
-// Persistent hemv blocks: HL_BPS per SM of the current device.
-static int hemv_blocks() { return device_sms() * HL_BPS; }
+// Persistent hemv blocks: bps per SM of the current device (at most HL_BPS,
+// the residency the kernel is compiled for).
+static int hemv_blocks(int bps) { return device_sms() * std::max(1, std::min(bps, HL_BPS)); }
 
 template <class R>
 cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
@@ -564,7 +565,7 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
                             A, lda, sA, w.nvec, i, nparts, w.nrm, w.nrb, w.e, w.tau, sd, w.scal)));
       const int m = nmax - i - 1;
       const int nt = cdiv(m, HL_T);
-      PP_KT(KT_HEMV, s, (k_hemv_lower<R><<<dim3(std::min(nt * (nt + 1) / 2, hemv_blocks()), 1, B), HL_NT, 0, s>>>(
+      PP_KT(KT_HEMV, s, (k_hemv_lower<R><<<dim3(std::min(nt * (nt + 1) / 2, hemv_blocks(w.hemv_bps)), 1, B), HL_NT, 0, s>>>(
                             A, lda, sA, w.nvec, i, P, sP, lda)));
       if (jj > 0) PP_KT(KT_DOTS, s, (k_dots<R><<<dim3(2 * jj, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb)));
       const int nr = cdiv(m, TR_NT);
@@ -1142,8 +1143,7 @@ constexpr int GRAM_RCH = 64; // rows per chunk of the Gram product V^H V
 template <class R>
 __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Xb, int64_t ldx,
                                              int64_t sX, int x_is_v, const int *nvec, const int64_t *rng, int k0,
-                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp, int ncol_fixed, int rch,
-                                             int voff) {
+                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp, int ncol_fixed, int rch) {
   __shared__ C<R> sV[BT_RK][32];
   __shared__ C<R> sXt[BT_RK][BT_J];
   const int b = blockIdx.z;
@@ -1151,7 +1151,7 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
   const int ncol = x_is_v ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
   const int j0 = blockIdx.x * BT_J;
   const int ks = blockIdx.y;
-  const int rbeg = k0 + voff + ks * rch;
+  const int rbeg = k0 + 1 + ks * rch;
   if (j0 >= ncol || rbeg >= n) return;
   const C<R> *A = Ab + b * sA;
   const C<R> *X = x_is_v ? (A + lda * k0) : (Xb + b * sX);
@@ -1165,13 +1165,13 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
     for (int e = threadIdx.x; e < BT_RK * 32; e += 256) {
       const int a = e & 31, rr = e >> 5;
       const int r = r0 + rr;
-      sV[rr][a] = (a < jb && r < rend && r >= k0 + a + voff) ? cconj(A[r + lda * (k0 + a)]) : cz<R>();
+      sV[rr][a] = (a < jb && r < rend && r >= k0 + a + 1) ? cconj(A[r + lda * (k0 + a)]) : cz<R>();
     }
     for (int e = threadIdx.x; e < BT_RK * BT_J; e += 256) {
       const int jx = e & 63, rr = e >> 6;
       const int r = r0 + rr, j = j0 + jx;
       bool ok = r < rend && j < ncol;
-      if (x_is_v) ok = ok && r >= k0 + j + voff;
+      if (x_is_v) ok = ok && r >= k0 + j + 1;
       sXt[rr][jx] = ok ? X[r + ldX * j] : cz<R>();
     }
     __syncthreads();
@@ -1198,14 +1198,14 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
 template <class R>
 __global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int64_t sWp, const int *nvec,
                                               const int64_t *rng, int k0, int jb, int mode, z64 *G, const z64 *Tf,
-                                              C<R> *Wb, int64_t sWb, int ncol_fixed, int nks_fixed, int voff) {
+                                              C<R> *Wb, int64_t sWb, int ncol_fixed, int nks_fixed = 0) {
   __shared__ C<R> col[32][64];
   __shared__ z64 sT[32][32];
   const int b = blockIdx.y;
   const int n = nvec[b];
   const int ncol = mode == 0 ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
   // split-K partials to sum: one per BT_RCH rows, or nks_fixed
-  const int nks = nks_fixed > 0 ? (n - k0 - voff > 0 ? nks_fixed : 0) : (n - k0 - voff + BT_RCH - 1) / BT_RCH;
+  const int nks = nks_fixed > 0 ? (n - k0 - 1 > 0 ? nks_fixed : 0) : (n - k0 - 1 + BT_RCH - 1) / BT_RCH;
   if (mode != 0) {
     for (int e = threadIdx.x; e < 32 * 32; e += 64) sT[e / 32][e % 32] = Tf[b * 1024 + e];
   }
@@ -1235,12 +1235,11 @@ __global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int6
 // G = V^H V from the Gram partials of k_vhx (row chunks of GRAM_RCH, stored
 // 32 x 32 per chunk): one thread per entry.
 template <class R>
-__global__ void __launch_bounds__(1024) k_gram_sum(const C<R> *Wp, int64_t sWp, const int *nvec, int k0, z64 *G,
-                                                   int voff) {
+__global__ void __launch_bounds__(1024) k_gram_sum(const C<R> *Wp, int64_t sWp, const int *nvec, int k0, z64 *G) {
   const int b = blockIdx.x;
   const int n = nvec[b];
   const int a = threadIdx.x >> 5, j = threadIdx.x & 31;
-  const int nks = (n - k0 - voff + GRAM_RCH - 1) / GRAM_RCH;
+  const int nks = (n - k0 - 1 + GRAM_RCH - 1) / GRAM_RCH;
   C<R> s = cz<R>();
   for (int ks = 0; ks < nks; ++ks) s = cadd(s, Wp[b * sWp + ((int64_t)ks * 32 + a) * 32 + j]);
   G[b * 1024 + a * 32 + j] = cto64(s);
@@ -1285,14 +1284,13 @@ constexpr int AV_T = 64, AV_K = 16;
 template <class R>
 __global__ void __launch_bounds__(256) k_applyV(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Wb,
                                                 int64_t ldwp, int64_t sWb, C<R> *Eb, int64_t lde, int64_t sE,
-                                                const int *nvec, const int64_t *rng, int k0, int jb, int ncol_fixed,
-                                                int voff) {
+                                                const int *nvec, const int64_t *rng, int k0, int jb, int ncol_fixed) {
   __shared__ C<R> sV[AV_K][AV_T];
   __shared__ C<R> sY[AV_K][AV_T];
   const int b = blockIdx.z;
   const int n = nvec[b];
   const int m = ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2];
-  const int r0 = k0 + voff + blockIdx.x * AV_T, c0 = blockIdx.y * AV_T;
+  const int r0 = k0 + 1 + blockIdx.x * AV_T, c0 = blockIdx.y * AV_T;
   if (r0 >= n || c0 >= m) return;
   const C<R> *A = Ab + b * sA;
   const C<R> *Y = Wb + b * sWb;
@@ -1308,7 +1306,7 @@ __global__ void __launch_bounds__(256) k_applyV(const C<R> *Ab, int64_t lda, int
       const int x = e % AV_T, y = e / AV_T;
       const int a = kc + y;
       const int r = r0 + x, c = c0 + x;
-      sV[y][x] = (a < jb && r < n && r >= k0 + a + voff) ? A[r + lda * (k0 + a)] : cz<R>();
+      sV[y][x] = (a < jb && r < n && r >= k0 + a + 1) ? A[r + lda * (k0 + a)] : cz<R>();
       sY[y][x] = (a < jb && c < m) ? Y[(int64_t)a * ldwp + c] : cz<R>();
     }
     __syncthreads();
@@ -1339,19 +1337,11 @@ __global__ void __launch_bounds__(256) k_applyV(const C<R> *Ab, int64_t lda, int
     }
 }
 
-// Reflector columns of the panel starting at column k0.  One-stage layout
-// (voff = 1): column i's reflector has its unit at row i + 1, columns
-// 0 .. n-2.  Band layout (voff = 32, two-stage reduction): the panel's QR
-// reflector a has its unit at row k0 + 32 + a, min(32, n - k0 - 33) of them.
-static inline int panel_refl(const EigWork &w, int k0) {
-  if (w.voff == 1) return std::max(0, std::min(w.nb, w.nmax - 1 - k0));
-  return std::max(0, std::min(32, w.nmax - k0 - 33));
-}
-
 template <class R>
 cudaError_t back_transform(EigWork &w, cudaStream_t s) {
-  const int B = w.B, nmax = w.nmax, nb = w.nb, vo = w.voff;
+  const int B = w.B, nmax = w.nmax, nb = w.nb;
   if (nmax < 2) return cudaSuccess;
+  const int nref = nmax - 1;  // reflector columns 0 .. nmax-2
   const int64_t ldwp = w.ldwp;
   const int64_t sWp = (int64_t)w.ksplit * 32 * ldwp;
   const int64_t sWb = (int64_t)32 * ldwp;
@@ -1360,26 +1350,21 @@ cudaError_t back_transform(EigWork &w, cudaStream_t s) {
   C<R> *E = (C<R> *)w.E;
   C<R> *Wp = (C<R> *)w.Wp;
   C<R> *Wb = (C<R> *)w.Wb;
-  // second stage of a two-stage reduction first: E <- Q2 Z
-  if (w.band) PP_CUDA_TRY(apply_q2(w, E, w.lde, w.sE, w.mcap, 1, s));
-  int kstart = -1;
-  for (int k0 = 0; k0 < nmax; k0 += nb)
-    if (panel_refl(w, k0) > 0) kstart = k0;
+  const int kstart = ((nref - 1) / nb) * nb;
   for (int k0 = kstart; k0 >= 0; k0 -= nb) {
-    const int jb = panel_refl(w, k0);
-    if (jb <= 0) continue;
-    const int ks = cdiv(nmax - k0 - vo, BT_RCH);
-    const int ksg = cdiv(nmax - k0 - vo, GRAM_RCH);
+    const int jb = min(nb, nref - k0);
+    const int ks = cdiv(nmax - k0 - 1, BT_RCH);
+    const int ksg = cdiv(nmax - k0 - 1, GRAM_RCH);
     // Tf from G = V^H V
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, 32, sWp, 0, GRAM_RCH, vo)));
-    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G, vo)));
+    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, 32, sWp, 0, GRAM_RCH)));
+    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
     // Y = Tf V^H E ; E -= V Y
     PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
-                                                             jb, Wp, ldwp, sWp, 0, BT_RCH, vo)));
-    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, 0, 0, vo)));
-    PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - vo, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
-        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb, 0, vo)));
+                                                             jb, Wp, ldwp, sWp, 0, BT_RCH)));
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, 0)));
+    PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
+        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb, 0)));
     count_launch(6);
   }
   return cudaGetLastError();
@@ -1456,7 +1441,7 @@ __global__ void __launch_bounds__(256) k_xhz(const C<R> *Xb, int64_t ldx, int64_
 
 template <class R>
 cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaStream_t s) {
-  const int B = w.B, nmax = w.nmax, nb = w.nb, vo = w.voff;
+  const int B = w.B, nmax = w.nmax, nb = w.nb;
   if (nrows <= 0) return cudaSuccess;
   const int64_t ldx = w.lda, sX = (int64_t)w.lda * w.nbr;
   C<R> *A = (C<R> *)w.A;
@@ -1470,14 +1455,14 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
   k_rows_init<R><<<dim3(cdiv(nmax, 256), nrows, B), 256, 0, s>>>(X, ldx, sX, d_rows, nrows, w.nvec);
   count_launch(1);
   // X <- Q^H X = Q_last^H ... Q_0^H X: panels in forward order, Tf^H
-  for (int k0 = 0; k0 < nmax; k0 += nb) {
-    const int jb = panel_refl(w, k0);
-    if (jb <= 0) continue;
-    const int ks = cdiv(nmax - k0 - vo, BT_RCH);
-    const int ksg = cdiv(nmax - k0 - vo, GRAM_RCH);
+  const int nref = nmax - 1;
+  for (int k0 = 0; k0 < nref; k0 += nb) {
+    const int jb = min(nb, nref - k0);
+    const int ks = cdiv(nmax - k0 - 1, BT_RCH);
+    const int ksg = cdiv(nmax - k0 - 1, GRAM_RCH);
     PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb,
-                                                             Wp, 32, sWp, 0, GRAM_RCH, vo)));
-    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G, vo)));
+                                                             Wp, 32, sWp, 0, GRAM_RCH)));
+    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
     const bool tc = std::is_same<R, df>::value && w.tcS && tc_enabled();
     if (tc) {
@@ -1485,21 +1470,19 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
     } else {
       PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(nrows, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, X, ldx, sX, 0, w.nvec,
                                                                                w.rng, k0, jb, Wp, ldwp, sWp, nrows,
-                                                                               BT_RCH, vo)));
+                                                                               BT_RCH)));
     }
     PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(nrows, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 2,
                                                                           w.G, w.Tf, Wb, sWb, nrows,
-                                                                          tc ? vhx_tc_splits(w) : 0, vo)));
+                                                                          tc ? vhx_tc_splits(w) : 0)));
     if (tc) {
       PP_CUDA_TRY(applyV_tc(w, k0, jb, (zdf *)X, ldx, sX, (const zdf *)Wb, ldwp, sWb, nrows, s));
     } else {
-      PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - vo, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(
-                              A, w.lda, w.sA, Wb, ldwp, sWb, X, ldx, sX, w.nvec, w.rng, k0, jb, nrows, vo)));
+      PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(
+                              A, w.lda, w.sA, Wb, ldwp, sWb, X, ldx, sX, w.nvec, w.rng, k0, jb, nrows)));
     }
     count_launch(6);
   }
-  // second stage of a two-stage reduction: X <- Q2^H X
-  if (w.band) PP_CUDA_TRY(apply_q2(w, X, ldx, sX, nrows, 0, s));
   // Eb = X^H Z
   if (std::is_same<R, df>::value && w.tcS && tc_enabled()) {
     PP_CUDA_TRY(xhz_tc(w, (const zdf *)X, ldx, sX, nrows, (const zdf *)w.E, w.lde, w.sE, (zdf *)w.Eb,

@@ -24,7 +24,7 @@ int device_sms();
 // (pp_ktimer_enable / pp_ktimer_report).
 enum KClass {
   KT_ASSEMBLE = 0, KT_COLUPD, KT_REFL, KT_HEMV, KT_DOTS, KT_WCORR, KT_WFIN, KT_HER2K, KT_BISECT, KT_INVIT,
-  KT_VHX, KT_BTRED, KT_APPLYV, KT_VEL, KT_XHZ, KT_BANDQR, KT_BANDMV, KT_BULGE, KT_Q2, KT_N
+  KT_VHX, KT_BTRED, KT_APPLYV, KT_VEL, KT_XHZ, KT_N
 };
 extern unsigned kt_mask;
 void kt_begin(int k, cudaStream_t s);
@@ -47,8 +47,7 @@ struct EigWork {
   int nmax = 0;        // largest order
   int mcap = 0;        // eigenvector columns allocated per matrix
   int nb = 32;         // panel width
-  int voff = 1;        // row of a panel reflector's unit element: column + voff (1; 32 after a band reduction)
-  int band = 0;        // nonzero: two-stage reduction (the second stage's reflectors are in q2v / q2t)
+  int hemv_bps = 6;    // persistent blocks per SM of the Hermitian mat-vec (autotuned)
   int *nvec = nullptr; // [B] device: order of each matrix
 
   void *A = nullptr;   // [B][nmax*nmax]  D(q), overwritten by the reduction
@@ -98,20 +97,6 @@ struct EigWork {
   int *tcE = nullptr;     // [B][her2k_tc_exps(nmax)] (V, W) exponent pairs per row
   int64_t sTcE = 0;
   int *tcErr = nullptr;   // [B]
-
-  // two-stage reduction (mixed form): explicit panel V, V T, the hemm
-  // product / W panel, small per-panel products, the band, and the second
-  // stage's reflectors (v: 32 complex each, tau) in sweep order
-  void *Vb = nullptr;     // [B][lda*32]
-  void *Ub = nullptr;     // [B][lda*32]
-  void *Xb = nullptr;     // [B][lda*32]
-  z64 *Yp = nullptr;      // [B][nyp][32*32] partial V^H X
-  int nyp = 0;
-  z64 *Mb = nullptr;      // [B][32*32]
-  void *AB = nullptr;     // [B][64*nmax] lower band storage, 64 diagonals (band and bulge)
-  void *q2v = nullptr;    // [B][nq2*32]
-  z64 *q2t = nullptr;     // [B][nq2]
-  int64_t nq2 = 0;        // second-stage reflectors per matrix
 
   size_t bytes = 0;
 };
@@ -202,26 +187,6 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
 // assembled again into w.A.  sums: 3 * B * mcap doubles of scratch.
 cudaError_t error_estimates(const Geometry &g, const double *d_q, EigWork &w, int efmt, int raw_lambda,
                             double *sums, double *resid, double *werr, double *zerr, int64_t ldw, cudaStream_t s);
-
-// Two-stage reduction (mixed form, double-float storage, uniform order).
-// Stage 1: A -> band of 32 sub-diagonals (panel QR, tensor-core two-sided
-// trailing updates), the band copied to w.AB, the panel reflectors left in A
-// in the band layout (w.voff = 32).  Stage 2: bulge chasing to the real
-// tridiagonal (w.d, w.e), the reflectors kept in w.q2v / w.q2t.
-cudaError_t band_reduce(EigWork &w, cudaStream_t s);
-cudaError_t band_to_tridiag(EigWork &w, cudaStream_t s);
-// Number of second-stage reflectors for order n (bandwidth 32).
-int64_t q2_count(int64_t n);
-cudaError_t prepare_band();
-// X (n x ncols, ld ldx, matrix stride sX) <- Q2^H X (reverse = 0) or Q2 X
-// (reverse = 1: the reflectors in reverse order, for E = Q2 Z).
-cudaError_t apply_q2(EigWork &w, void *X, int64_t ldx, int64_t sX, int ncols, int reverse, cudaStream_t s);
-// Tensor-core pieces of stage 1 (pp_tc.cu):
-// X(k1 + c, j) = sum_r A22(c, r) U(r, j) over the full trailing square
-// (rows and columns >= k1), U = w.Ub rows >= k1, into w.Xb.
-cudaError_t band_hemm_tc(EigWork &w, int k1, cudaStream_t s);
-// A(k1:n, k1:n) -= V W^H + W V^H (lower triangle), V = w.Vb, W = w.Xb.
-cudaError_t band_her2k_tc(EigWork &w, int k1, cudaStream_t s);
 
 // Output conversion
 cudaError_t finalize_outputs(EigWork &w, int efmt, int raw_lambda, const double *d_vraw, int want_vel, int want_z,

@@ -732,70 +732,6 @@ static int take_stall(const EigWork &w, long long *cycles) {
   return b;
 }
 
-// Stage 1 of the two-stage reduction, hemm: X(k1 + c, j) = sum_r A22(c, r)
-// U(r, j) with A22 = A(k1:n, k1:n) held as a full Hermitian square, read
-// column-wise as conj(A22(r, c)) (long-K product, mode 0, one split), U the
-// explicit 32-column panel w.Ub (rows >= k1).
-cudaError_t band_hemm_tc(EigWork &w, int k1, cudaStream_t s) {
-  const int m = w.nmax - k1;
-  if (m <= 0) return cudaSuccess;
-  const int64_t sP = w.lda * 32;
-  LongK p{};
-  p.A = (const zdf *)w.A + w.lda * k1;
-  p.lda = w.lda;
-  p.sA = w.sA;
-  p.conj_a = 1;
-  p.Bm = (const zdf *)w.Ub;
-  p.ldb = w.lda;
-  p.sB = sP;
-  p.conj_b = 1;
-  p.vmask = 0;
-  p.k0 = k1 - 32;  // 32 valid columns of U (zero beyond the panel's reflectors)
-  p.jb = 32;
-  p.rbeg = k1;
-  p.ncols_a = m;
-  p.out = (zdf *)w.Xb + k1;
-  p.ldo = w.lda;
-  p.sO = sP;
-  p.mode = 0;
-  PP_KT(KT_HER2K, s, (k_longk_tc<<<dim3((m + 127) / 128, 1, w.B), TC_NT, VX_SMEM, s>>>(p, w.nvec, w.tcErr)));
-  count_launch(1);
-  return cudaGetLastError();
-}
-
-// Stage 1, trailing update: A(k1:n, k1:n) -= V W^H + W V^H (lower
-// triangle), V = w.Vb and W = w.Xb explicit 32-column panels.
-cudaError_t band_her2k_tc(EigWork &w, int k1, cudaStream_t s) {
-  const int mmax = w.nmax - k1;
-  if (mmax <= 0) return cudaSuccess;
-  const int64_t sP = w.lda * 32;
-  const int km = k1 - 32;  // all 32 columns valid
-  PP_CUDA_TRY(launch_slices(TcSliceSrc{(const zdf *)w.Vb, sP, 1, w.lda, k1, 0, 0, 0}, mmax, w, km, 32, w.tcS,
-                            TC_RBLK, w.tcE, 2, 0, s));
-  PP_CUDA_TRY(launch_slices(TcSliceSrc{(const zdf *)w.Xb, sP, 1, w.lda, k1, 0, 0, 0}, mmax, w, km, 32,
-                            w.tcS + TC_OP, TC_RBLK, w.tcE, 2, 1, s));
-  TcUpdate u{};
-  u.C = (zdf *)w.A;
-  u.ldc = w.lda;
-  u.sC = w.sA;
-  u.rbase = u.cbase = k1;
-  u.ncols_fixed = 0;
-  u.tri = 1;
-  u.nprod = 2;
-  const TcOperand V{w.tcS, w.sTcS, TC_RBLK, w.tcE, w.sTcE, 2, 0};
-  const TcOperand Wo{w.tcS + TC_OP, w.sTcS, TC_RBLK, w.tcE, w.sTcE, 2, 1};
-  u.x[0] = V;
-  u.y[0] = Wo;
-  u.x[1] = Wo;
-  u.y[1] = V;
-  u.stall_b = -1;
-  const int nrb = (mmax + 127) / 128;
-  const int nq = (4 * nrb + TC_CB - 1) / TC_CB;
-  PP_KT(KT_HER2K, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>(u, w.nvec, w.tcErr)));
-  count_launch(1);
-  return cudaGetLastError();
-}
-
 // A(k1:n, k1:n) -= V W^H + W V^H, lower triangle (panel k0 of width jb).
 cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s) {
   const int k1 = k0 + jb;
@@ -835,18 +771,15 @@ cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s) {
 // back-transform as X Y'^H with Y'(c, a) = conj(Y(a, c)).
 cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t sX, const zdf *Yb, int64_t ldy,
                       int64_t sY, int ncols, cudaStream_t s) {
-  // rows from the first unit row; the slicing masks V above row
-  // k0 + voff + a by its panel offset k0 + voff - 1
-  const int r1 = k0 + w.voff;
-  const int km = k0 + w.voff - 1;
+  const int r1 = k0 + 1;
   const int mmax = w.nmax - r1;
   if (mmax <= 0 || ncols <= 0) return cudaSuccess;
   const zdf *A = (const zdf *)w.A;
   const int64_t vbl = (int64_t)((w.nmax + 127) / 128) * TC_OP;  // the Y' slices follow the V slices
   const int64_t yexp = (w.nmax + 127) / 128 * 128;
-  PP_CUDA_TRY(launch_slices(TcSliceSrc{A + w.lda * k0, w.sA, 1, w.lda, r1, 0, 1, 0}, mmax, w, km, jb, w.tcS, TC_OP,
+  PP_CUDA_TRY(launch_slices(TcSliceSrc{A + w.lda * k0, w.sA, 1, w.lda, r1, 0, 1, 0}, mmax, w, k0, jb, w.tcS, TC_OP,
                             w.tcE, 1, 0, s));
-  PP_CUDA_TRY(launch_slices(TcSliceSrc{Yb, sY, 1, ldy, 0, ncols, 0, 1}, ncols, w, km, jb, w.tcS + vbl, TC_OP,
+  PP_CUDA_TRY(launch_slices(TcSliceSrc{Yb, sY, 1, ldy, 0, ncols, 0, 1}, ncols, w, k0, jb, w.tcS + vbl, TC_OP,
                             w.tcE + yexp, 1, 0, s));
   TcUpdate u{};
   u.C = X;
@@ -884,9 +817,9 @@ cudaError_t vhx_tc(EigWork &w, int k0, int jb, const zdf *X, int64_t ldx, int64_
   p.ldb = w.lda;
   p.sB = w.sA;
   p.vmask = 1;
-  p.k0 = k0 + w.voff - 1;  // mask: rows >= k0 + voff + j
+  p.k0 = k0;
   p.jb = jb;
-  p.rbeg = k0 + w.voff;
+  p.rbeg = k0 + 1;
   p.ncols_a = ncols;
   p.out = Wp;
   p.ldo = ldwp;
