@@ -300,6 +300,7 @@ def main():
         extra["fp64_form"] = {"value": Bf / t64, "unit": UNIT, "q_per_step": Bf,
                               "note": "same pipeline, IEEE double in every stage; host API, one step"}
         extra["mixed_over_fp64"] = None  # filled below from e2e-comparable numbers
+        extra["library_fp64_context"] = cusolver_context(ctx, qf[:2], dev)
         extra["accuracy"] = {"max_abs_dw_cm1_mixed_vs_fp64": dw, "max_dv_rel_per_mode_mixed_vs_fp64": dv,
                              "q_compared": Bf,
                              "rule": "modes with |w| >= 1 cm^-1; velocities per mode relative to "
@@ -514,6 +515,27 @@ def other_configs(dev):
     finally:
         spec.close()
     return res
+
+
+def cusolver_context(ctx, qs, dev):
+    """Context only (not on the product path): the same D(q) handed to the
+    vendor library's FP64 Hermitian eigensolver (torch.linalg.eigvalsh /
+    eigh on complex128, cuSOLVER heevd) on this GPU, seconds per q-point."""
+    import torch
+    out = {"note": "cuSOLVER heevd through torch.linalg on the library's D(q); no velocities; context for the "
+                   "FP64 form, not a baseline of the metric"}
+    Ds = [torch.as_tensor(ctx.dynamical_matrix(q), device=dev) for q in qs]
+    for name, fn in (("eigvalsh_s_per_q", torch.linalg.eigvalsh), ("eigh_s_per_q", torch.linalg.eigh)):
+        fn(Ds[0])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for D in Ds:
+            fn(D)
+        torch.cuda.synchronize()
+        out[name] = (time.perf_counter() - t0) / len(Ds)
+    del Ds
+    torch.cuda.empty_cache()
+    return out
 
 
 def cpu_baseline(cell, phi, q_all):
