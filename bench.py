@@ -412,7 +412,14 @@ def timed(fn, nq, n, kclasses=ALL_KERNELS):
     roof = None
     if kt:
         dom = max(kt, key=lambda k: kt[k][1])
-        roof = roofline_for(dom, kt[dom], n, nq)
+        if isinstance(n, (list, tuple)):   # cells of several orders: (order, q-points) pairs
+            parts = [roofline_for(dom, kt[dom], ni, qi) for ni, qi in n]
+            roof = dict(parts[0])
+            if roof.get("achieved") is not None:
+                roof["achieved"] = sum(pp["achieved"] for pp in parts)
+                roof["frac"] = roof["achieved"] / roof["peak"] if roof.get("peak") else None
+        else:
+            roof = roofline_for(dom, kt[dom], n, nq)
         roof = {k: roof.get(k) for k in ("kernel", "bound", "achieved", "unit", "frac", "peak")}
         roof["share_of_kernel_time"] = round(kt[dom][1] / sum(v[1] for v in kt.values()), 3)
     return out, {"value": nq / dt, "unit": UNIT, "s": dt, "n_q": nq, "roofline": roof}
@@ -484,7 +491,8 @@ def other_configs(dev):
         cell_of = np.repeat(np.arange(3), len(g))
         o = api.EigOpts(jobz="N", vel=True, precision=api.PP_PREC_MIXED)
         api.solve_multi(ctxs, cell_of[:6], q[:6], o, want_z=False)
-        r, e = timed(lambda: api.solve_multi(ctxs, cell_of, q, o, want_z=False), len(q), cells[2].n)
+        r, e = timed(lambda: api.solve_multi(ctxs, cell_of, q, o, want_z=False), len(q),
+                     [(cc.n, len(g)) for cc in cells])
         e.update({"workload": "N=148/364/868 in shared batches, Gamma-centred grids, w + v_g, mixed",
                   "sample": "8x8 grid per cell (64 q each, 192 q) of the 32x32 grids"})
         res["3_uneven_cells"] = e

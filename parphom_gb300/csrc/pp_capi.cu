@@ -526,15 +526,17 @@ bool graphs_enabled() {
 // run_batch through a captured CUDA graph: the launch sequence depends only on
 // the batch size, the options and the workspace, so it is captured once and
 // replayed (one graph launch instead of ~6 launches per matrix column).
-int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z);
+int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z, bool launch = true);
 
-// Time one launch configuration: capture its graph and time its launch on
-// the stream.  Returns the milliseconds, or a negative value if the graph
-// path is not available.
+// Time one launch configuration: capture and instantiate its graph (host
+// work, not timed), then time one launch of it on the stream with events.
+// Returns the milliseconds, or a negative value if the graph path is not
+// available.
 float time_config(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z, int split, int bps) {
   c->cur_split = split;
   c->cur_bps = bps;
   cudaStream_t s = c->stream;
+  if (run_batch_graph_cfg(c, B, o, mcap, want_z, false) != PP_OK || !c->gexec) return -1.f;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
     cudaGetLastError();
@@ -542,12 +544,11 @@ float time_config(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z,
     return -1.f;
   }
   float ms = -1.f;
-  // one launch: the capture and instantiation before it are host work (a
-  // small gap on the GPU timeline next to a batch of seconds)
   cudaEventRecord(e0, s);
-  const int r = run_batch_graph_cfg(c, B, o, mcap, want_z);
+  const cudaError_t r = cudaGraphLaunch(c->gexec, s);
+  pp::count_launch(c->glaunches);
   cudaEventRecord(e1, s);
-  if (r == PP_OK && c->gexec && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  if (r == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
   cudaGetLastError();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -598,15 +599,19 @@ int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_
   return run_batch_graph_cfg(c, B, o, mcap, want_z);
 }
 
-int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z) {
+// The batch through its captured graph (captured on the first use of a
+// configuration); with launch = false the graph is only captured and
+// instantiated (used by the autotuner, which then times the launch).
+int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_z, bool launch) {
   // (an armed test stall is a one-shot launch parameter: never captured)
-  if (!graphs_enabled() || pp::kt_mask || tc_stall_armed()) return run_batch(c, B, o, mcap, want_z);
+  if (!graphs_enabled() || pp::kt_mask || tc_stall_armed()) return launch ? run_batch(c, B, o, mcap, want_z) : 1;
   char key[192];
   snprintf(key, sizeof(key), "%p|%d|%d|%c%c%c|%d|%lld|%lld|%.17g|%.17g|%.17g|%d|%d|%d|%d", c->ws, B, o->precision,
            o->jobz, o->range, o->vel_method, o->vel, (long long)o->il, (long long)o->iu, o->vl, o->vu, o->abstol,
            want_z ? 1 : 0, c->cur_split, c->cur_bps, o->want_resid ? 1 : 0);
   cudaStream_t s = c->stream;
   if (c->gexec && strcmp(key, c->gkey) == 0) {
+    if (!launch) return PP_OK;
     TRY_CUDA(cudaGraphLaunch(c->gexec, s));
     pp::count_launch(c->glaunches);
     return PP_OK;
@@ -615,7 +620,7 @@ int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool w
   TRY_CUDA(prepare_bisect(bisect_smem(c->w.nmax, o->precision == PP_PREC_MIXED)));
   if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
     cudaGetLastError();
-    return run_batch(c, B, o, mcap, want_z);
+    return launch ? run_batch(c, B, o, mcap, want_z) : 1;
   }
   const int64_t l0 = pp::g_launches.load();
   const int r = run_batch(c, B, o, mcap, want_z);
@@ -625,16 +630,20 @@ int run_batch_graph_cfg(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool w
   if (r != PP_OK || e != cudaSuccess || !g) {
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
-    return run_batch(c, B, o, mcap, want_z);
+    return launch ? run_batch(c, B, o, mcap, want_z) : 1;
   }
   e = cudaGraphInstantiate(&c->gexec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
     c->gexec = nullptr;
     cudaGetLastError();
-    return run_batch(c, B, o, mcap, want_z);
+    return launch ? run_batch(c, B, o, mcap, want_z) : 1;
   }
   snprintf(c->gkey, sizeof(c->gkey), "%s", key);
+  if (!launch) {
+    pp::g_launches.fetch_sub(c->glaunches);  // captured, not launched
+    return PP_OK;
+  }
   TRY_CUDA(cudaGraphLaunch(c->gexec, s));
   return PP_OK;
 }

@@ -1359,13 +1359,22 @@ cudaError_t back_transform(EigWork &w, cudaStream_t s) {
     PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, 32, sWp, 0, GRAM_RCH)));
     PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
     k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
-    // Y = Tf V^H E ; E -= V Y
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
-                                                             jb, Wp, ldwp, sWp, 0, BT_RCH)));
-    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, 0)));
-    PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
-        A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb, 0)));
-    count_launch(6);
+    // Y = Tf V^H E ; E -= V Y (on the tensor cores in the double-float form,
+    // over all mcap columns)
+    const bool tc = std::is_same<R, df>::value && w.tcS && tc_enabled();
+    if (tc) {
+      PP_CUDA_TRY(vhx_tc(w, k0, jb, (const zdf *)E, w.lde, w.sE, w.mcap, (zdf *)Wp, ldwp, sWp, s));
+      PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, w.mcap, vhx_tc_splits(w))));
+      PP_CUDA_TRY(applyV_tc(w, k0, jb, (zdf *)E, w.lde, w.sE, (const zdf *)Wb, ldwp, sWb, w.mcap, s));
+      count_launch(4);
+    } else {
+      PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
+                                                               jb, Wp, ldwp, sWp, 0, BT_RCH)));
+      PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, 0)));
+      PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
+          A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb, 0)));
+      count_launch(6);
+    }
   }
   return cudaGetLastError();
 }
