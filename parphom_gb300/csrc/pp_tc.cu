@@ -21,12 +21,11 @@
 // both at full relative resolution; the dropped pairs and the residual bound
 // the error by about 2^-55 |X_r| |Y_c| per product, the double-float level.
 //
-// CTA (512 threads) = 128 rows x (up to 16) column blocks of 16, both
+// CTA (512 threads) = 128 rows x (up to 8) column blocks of 32, both
 // products in turn.  The 112 KB row operand stays in shared memory while the
-// 14 KB column operands are streamed in by bulk copies, double-buffered;
-// the accumulators are double-buffered in tensor memory so that one block's
-// MMAs run during the previous block's epilogue.  One CTA per SM (141 KB of
-// shared memory, 448 of the 512 tensor-memory columns).
+// 28 KB column operands are streamed in by bulk copies, double-buffered so
+// that the next block's copy overlaps this block's MMAs.  One CTA per SM
+// (168 KB of shared memory, 448 tensor-memory columns).
 #include <algorithm>
 #include <cfloat>
 #include <cstdint>
@@ -47,8 +46,10 @@ constexpr int TC_TILE = 4096;                    // one (slice, k-step) tile of 
 constexpr int TC_OP = TC_S * TC_KS * TC_TILE;    // one operand of a 128-row block (114688)
 constexpr int TC_RBLK = 2 * TC_OP;               // V and W operands of a 128-row block
 constexpr int TC_BBYTES = TC_S * TC_KS * 1024;   // one 32-row column block of one operand (28672)
+constexpr int TC_CB = 8;                         // column blocks per CTA
 constexpr int TC_NT = 512;                       // threads: 16 warps = 4 lane groups x 4 column quarters
 constexpr int TC_CQ = 32 / (TC_NT / 128);        // columns per thread in the epilogue (8)
+constexpr int TC_SMEM = TC_OP + 2 * TC_BBYTES + 2 * 256 + 64;  // + 2 x 32 exponent pairs, mbarriers, TMEM slot
 constexpr int TC_NACC = 2 * TC_S;                // accumulators: (re, im) x slice-sum group
 constexpr uint32_t TC_ID = tc::idesc_bf16(128, 32, 0);
 constexpr uint32_t TC_IDN = tc::idesc_bf16(128, 32, 1);
@@ -196,69 +197,28 @@ struct TcUpdate {
   long long stall_cycles;
 };
 
-// The tile update runs on column blocks of 16 with two accumulator sets in
-// tensor memory (2 x 14 x 16 of the 512 columns): the MMAs of block i + 1
-// are issued before the double-float epilogue of block i, so the tensor
-// cores work while the CUDA cores fold, scale and subtract.  The column
-// operand is double-buffered (bulk copies), its exponents triple-buffered
-// (the copy for block i + 2 starts once block i's MMAs are done, while block
-// i's epilogue still reads its exponents).  The row operand (one 128-row
-// block, 112 KB) is reloaded between the two products of a launch.
-constexpr int TU_NB = 16;                            // columns per block
-constexpr int TU_BBYTES = TC_S * TC_KS * 512;        // one 16-row column block of one operand (14336)
-constexpr int TU_CB = 16;                            // column blocks per CTA
-constexpr int TU_CQ = TU_NB / (TC_NT / 128);         // columns per thread in the epilogue (4)
-constexpr int TU_SET = TC_NACC * TU_NB;              // tensor-memory columns of one accumulator set (224)
-constexpr int TU_EB = 3;                             // exponent slots
-constexpr int TU_ESLOT = TU_NB * 2;                  // ints per exponent slot (up to 2 per column)
-constexpr int TU_SMEM = TC_OP + 2 * TU_BBYTES + TU_EB * TU_ESLOT * 4 + 128;
-constexpr uint32_t TU_ID = tc::idesc_bf16(128, 16, 0);
-constexpr uint32_t TU_IDN = tc::idesc_bf16(128, 16, 1);
-static_assert(2 * TU_SET <= 512, "two accumulator sets fit tensor memory");
-static_assert(TC_NT == 32 * 4 * (TU_NB / TU_CQ), "epilogue: 4 lane groups x column quarters");
-
-// tc_issue for a 16-column block into accumulator set tm.
-__device__ __forceinline__ void tu_issue(uint32_t tm, uint32_t sa, uint32_t sb) {
-  const uint64_t a0 = tc::sdesc(sa, 128, 256), b0 = tc::sdesc(sb, 128, 256);
-#pragma unroll
-  for (int u = 0; u < TC_S; ++u) {
-#pragma unroll
-    for (int s = 0; s <= u; ++s) {
-      const int t = u - s;
-#pragma unroll
-      for (int j = 0; j < TC_KS; ++j) {
-        const uint32_t acc = (s == 0 && j == 0) ? 0u : 1u;
-        const uint64_t ad = a0 + (uint64_t)((s * TC_KS + j) * (TC_TILE >> 4));
-        const uint64_t br = b0 + (uint64_t)((t * TC_KS + j) * (512 >> 4));
-        const uint64_t bi = b0 + (uint64_t)((t * TC_KS + (j ^ 2)) * (512 >> 4));
-        tc::mma_bf16(tm + u * TU_NB, ad, br, TU_ID, acc);
-        tc::mma_bf16(tm + (TC_S + u) * TU_NB, ad, bi, j < 2 ? TU_IDN : TU_ID, acc);
-      }
-    }
-  }
-}
-
 __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nvec, int *err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *sAop = smem;                                   // row operand
-  uint8_t *sBop = smem + TC_OP;                           // two column-operand buffers
-  int *sEc = (int *)(smem + TC_OP + 2 * TU_BBYTES);       // TU_EB exponent slots
-  // mbarriers: [0] row operand landed, [1], [2] column buffer 0 / 1 landed,
-  // [3], [4] MMAs into accumulator set 0 / 1 done, [5] never completed (the
-  // test hook's wait).  Thread 0 counts, per barrier, the phases it started
-  // and the ones it has seen complete; the k-th completion has parity k & 1.
-  uint64_t *bars = (uint64_t *)(smem + TC_OP + 2 * TU_BBYTES + TU_EB * TU_ESLOT * 4);
-  uint32_t *tslot = (uint32_t *)(bars + 6);
+  uint8_t *sAop = smem;                                  // row operand
+  uint8_t *sBop = smem + TC_OP;                          // two column-operand buffers
+  int *sEc = (int *)(smem + TC_OP + 2 * TC_BBYTES);      // two x 64 column exponents
+  // mbarriers: [0] row operand landed (waited by thread 0), [1], [2] column
+  // buffer 0 / 1 landed, [3] MMAs of the block done, [4] never arrived on
+  // (the test hook's wait).
+  // Each barrier a thread waits on completes exactly once between two of
+  // its waits, so parity waits cannot skip a phase.
+  uint64_t *bars = (uint64_t *)(smem + TC_OP + 2 * TC_BBYTES + 512);
+  uint32_t *tslot = (uint32_t *)(bars + 5);
   const int b = blockIdx.z, R = blockIdx.y, q = blockIdx.x;
   const int n = nvec[b];
   const int nrows = n - u.rbase;
   const int ncols = u.ncols_fixed > 0 ? u.ncols_fixed : n - u.cbase;
   if (nrows <= 0 || ncols <= 0) return;
-  const int nrb = (nrows + 127) / 128, ncb = (ncols + TU_NB - 1) / TU_NB;
+  const int nrb = (nrows + 127) / 128, ncb = (ncols + 31) / 32;
   if (R >= nrb) return;
-  const int cb_beg = q * TU_CB;
-  int cb_end = min(cb_beg + TU_CB, ncb);
-  if (u.tri) cb_end = min(cb_end, (128 / TU_NB) * (R + 1));
+  const int cb_beg = q * TC_CB;
+  int cb_end = min(cb_beg + TC_CB, ncb);
+  if (u.tri) cb_end = min(cb_end, 4 * (R + 1));
   if (cb_beg >= cb_end) return;
   // an earlier wait of this matrix gave up: its results are already invalid
   if (*(volatile int *)&err[b]) return;
@@ -268,7 +228,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) tc::tmem_alloc(tslot, 512);
   if (tid == 0) {
-    for (int i = 0; i < 6; ++i) tc::mbar_init(&bars[i], 1);
+    for (int i = 0; i < 5; ++i) tc::mbar_init(&bars[i], 1);
     tc::mbar_init_fence();
   }
   tc::fence_before();
@@ -279,145 +239,129 @@ __global__ void __launch_bounds__(TC_NT, 1) k_cupd_tc(TcUpdate u, const int *nve
   zdf *C = u.C + b * u.sC;
   const int r0 = u.rbase + 128 * R;  // first global row of this row block
   const int nr = min(128, nrows - 128 * R);
-  const uint32_t sa = tc::smem_u32(sAop);
-  int iss[5] = {0, 0, 0, 0, 0}, wtd[5] = {0, 0, 0, 0, 0};  // thread 0's phase counts
-  bool good = true;                                        // thread 0: every wait so far succeeded
-  auto issue_row = [&](int p) {
-    const TcOperand &x = u.x[p];
-    tc::mbar_expect_tx(&bars[0], TC_OP);
-    const uint8_t *src = x.S + b * x.sS + (int64_t)R * x.blk;
-    for (int s = 0; s < TC_S; ++s)
-      tc::bulk_g2s(sAop + s * (TC_KS * TC_TILE), src + s * (TC_KS * TC_TILE), TC_KS * TC_TILE, &bars[0]);
-    ++iss[0];
-  };
+  // column operand of step i (product i / ncbw, column block cb)
   auto issue_cols = [&](int i) {
     const TcOperand &y = u.y[i / ncbw];
     const int cb = cb_beg + i % ncbw;
     const int buf = i & 1;
     uint64_t *bar = &bars[1 + buf];
-    const uint32_t ebytes = (uint32_t)TU_NB * 4u * (uint32_t)y.es;
-    tc::mbar_expect_tx(bar, TU_BBYTES + ebytes);
-    const uint8_t *src = y.S + b * y.sS + (int64_t)(cb >> 3) * y.blk + (cb & 7) * 512;
-    uint8_t *dst = sBop + buf * TU_BBYTES;
-    for (int sj = 0; sj < TC_S * TC_KS; ++sj) tc::bulk_g2s(dst + sj * 512, src + sj * TC_TILE, 512, bar);
-    tc::bulk_g2s(sEc + (i % TU_EB) * TU_ESLOT, y.E + b * y.sE + (int64_t)TU_NB * cb * y.es, ebytes, bar);
-    ++iss[1 + buf];
+    const uint32_t ebytes = 32u * 4u * (uint32_t)y.es;
+    tc::mbar_expect_tx(bar, TC_BBYTES + ebytes);
+    const uint8_t *src = y.S + b * y.sS + (int64_t)(cb >> 2) * y.blk + (cb & 3) * 1024;
+    uint8_t *dst = sBop + buf * TC_BBYTES;
+    for (int sj = 0; sj < TC_S * TC_KS; ++sj) tc::bulk_g2s(dst + sj * 1024, src + sj * TC_TILE, 1024, bar);
+    tc::bulk_g2s(sEc + buf * 64, y.E + b * y.sE + (int64_t)32 * cb * y.es, ebytes, bar);
   };
-  // MMAs of step i into accumulator set i & 1 (thread 0), after its copies landed
-  auto issue_mma = [&](int i) {
-    const int buf = i & 1;
-    if (good && i % ncbw == 0) {
-      good = tc::mbar_wait(&bars[0], (uint32_t)(wtd[0] & 1));
-      if (good) ++wtd[0];
-    }
-    if (good) {
-      good = tc::mbar_wait(&bars[1 + buf], (uint32_t)(wtd[1 + buf] & 1));
-      if (good) ++wtd[1 + buf];
-    }
-    if (good) {
-      tc::fence_after();
-      tu_issue(tm + (uint32_t)(buf * TU_SET), sa, tc::smem_u32(sBop + buf * TU_BBYTES));
-    }
-    tc::mma_commit(&bars[3 + buf]);
-    ++iss[3 + buf];
-  };
-  if (tid == 0) {
-    issue_row(0);
-    issue_cols(0);
-    if (nblk > 1) issue_cols(1);
-    if (stall) good = tc::mbar_wait(&bars[5], 0u, u.stall_cycles);
-    issue_mma(0);
-  }
   const int lg = warp & 3, cqt = warp >> 2;
   const int rl = 128 * R + 32 * lg + (tid & 31);  // row within the block of rows = TMEM lane
   const int r = u.rbase + rl;
   int erow[2] = {0, 0};
   for (int p = 0; p < u.nprod; ++p) erow[p] = u.x[p].E[b * u.x[p].sE + (int64_t)rl * u.x[p].es + u.x[p].eo];
-  int ok = 1;
+  const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + TC_CQ * cqt;
+  const uint32_t sa = tc::smem_u32(sAop);
+  int ok = 1, failed_i = -1;
   for (int i = 0; i < nblk; ++i) {
-    const int p = i / ncbw, cb = cb_beg + i % ncbw, set = i & 1;
-    // next block's MMAs ahead of this block's epilogue (not across the
-    // product boundary: the row operand is reloaded there)
-    if (tid == 0 && i + 1 < nblk && (i + 1) % ncbw != 0) issue_mma(i + 1);
-    if (tid == 0 && p == 0 && i + 1 < ncbw) {  // the next block's columns of C towards L2
-      const int c0 = u.cbase + TU_NB * (cb + 1);
-      for (int c = c0; c < min(c0 + TU_NB, u.cbase + ncols); ++c)
-        tc::prefetch_l2(C + r0 + u.ldc * c, (uint32_t)nr * 16u);
+    const int p = i / ncbw, cb = cb_beg + i % ncbw;
+    const uint32_t par3 = (uint32_t)(i & 1);
+    bool good = true;  // thread 0: every copy landed and every MMA was issued
+    if (tid == 0) {
+      if (i % ncbw == 0) {
+        // row operand of product p (the previous product's MMAs are done)
+        const TcOperand &x = u.x[p];
+        tc::mbar_expect_tx(&bars[0], TC_OP);
+        const uint8_t *src = x.S + b * x.sS + (int64_t)R * x.blk;
+        for (int s = 0; s < TC_S; ++s)
+          tc::bulk_g2s(sAop + s * (TC_KS * TC_TILE), src + s * (TC_KS * TC_TILE), TC_KS * TC_TILE, &bars[0]);
+      }
+      if (i == 0) issue_cols(0);
+      if (i + 1 < nblk) issue_cols(i + 1);
+      if (p == 0 && i + 1 < ncbw) {  // the next tile of C towards L2
+        const int c0 = u.cbase + 32 * (cb + 1);
+        for (int c = c0; c < min(c0 + 32, u.cbase + ncols); ++c)
+          tc::prefetch_l2(C + r0 + u.ldc * c, (uint32_t)nr * 16u);
+      }
+      if (i == 0 && stall) good = tc::mbar_wait(&bars[4], 0u, u.stall_cycles);
+      if (i % ncbw == 0) good = good && tc::mbar_wait(&bars[0], (uint32_t)p);
+      good = good && tc::mbar_wait(&bars[1 + (i & 1)], (uint32_t)((i >> 1) & 1));
+      if (good) {
+        tc::fence_after();
+        tc_issue(tm, sa, tc::smem_u32(sBop + (i & 1) * TC_BBYTES));
+      }
+      tc::mma_commit(&bars[3]);
+      if (!good) atomicExch(&err[b], 1);
     }
     // this thread's entries of C, loaded while the MMAs run
-    zdf cv[TU_CQ];
-    const int cl0 = TU_NB * cb + TU_CQ * cqt;  // first column (local) of this thread
+    zdf cv[TC_CQ];
+    const int cl0 = 32 * cb + TC_CQ * cqt;  // first column (local) of this thread
 #pragma unroll
-    for (int qq = 0; qq < TU_CQ; ++qq) {
+    for (int qq = 0; qq < TC_CQ; ++qq) {
       const int cl = cl0 + qq, c = u.cbase + cl;
       if (rl < nrows && cl < ncols && (!u.tri || r >= c)) cv[qq] = C[r + u.ldc * c];
     }
-    bool done = tc::mbar_wait(&bars[3 + set], (uint32_t)((i >> 1) & 1));
+    bool done = tc::mbar_wait(&bars[3], par3);
     // (already complete: makes the copied column exponents visible here)
-    done = done && tc::mbar_wait(&bars[1 + set], (uint32_t)((i >> 1) & 1));
-    if (tid == 0) {
-      if (done) wtd[3 + set] = (i >> 1) + 1;
-      // block i's MMAs are done: its column buffer takes block i + 2
-      if (good && done && i + 2 < nblk) issue_cols(i + 2);
-      // product boundary: reload the row operand, then the next product's first MMAs
-      if (good && done && i + 1 < nblk && (i + 1) % ncbw == 0) {
-        issue_row(p + 1);
-        issue_mma(i + 1);
-      }
+    done = done && tc::mbar_wait(&bars[1 + (i & 1)], (uint32_t)((i >> 1) & 1));
+    ok = __syncthreads_and(done && ok && good);
+    if (!ok) {
+      failed_i = i;
+      break;
     }
-    ok = __syncthreads_and(done && ok && (tid != 0 || good));
-    if (!ok) break;
     tc::fence_after();
     const int er = erow[p];
     const TcOperand &y = u.y[p];
-    const int *ec = sEc + (i % TU_EB) * TU_ESLOT;
-    const uint32_t lane_addr = tm + ((uint32_t)(32 * lg) << 16) + (uint32_t)(set * TU_SET) + TU_CQ * cqt;
-    float are[TC_S][4], aim[TC_S][4];
+    const int *ec = sEc + (i & 1) * 64;
 #pragma unroll
-    for (int uu = 0; uu < TC_S; ++uu) {
-      tc::tmem_ld4(lane_addr + uu * TU_NB, are[uu]);
-      tc::tmem_ld4(lane_addr + (TC_S + uu) * TU_NB, aim[uu]);
-    }
-    tc::tmem_ld_wait();
+    for (int cc = 0; cc < TC_CQ / 4; ++cc) {
+      float are[TC_S][4], aim[TC_S][4];
 #pragma unroll
-    for (int qq = 0; qq < TU_CQ; ++qq) {
-      const int cl = cl0 + qq, c = u.cbase + cl;
-      if (rl < nrows && cl < ncols && (!u.tri || r >= c)) {
-        float vr[TC_S], vi[TC_S];
+      for (int uu = 0; uu < TC_S; ++uu) {
+        tc::tmem_ld4(lane_addr + uu * 32 + cc * 4, are[uu]);
+        tc::tmem_ld4(lane_addr + (TC_S + uu) * 32 + cc * 4, aim[uu]);
+      }
+      tc::tmem_ld_wait();
 #pragma unroll
-        for (int uu = 0; uu < TC_S; ++uu) {
-          vr[uu] = are[uu][qq];
-          vi[uu] = aim[uu][qq];
+      for (int qq = 0; qq < 4; ++qq) {
+        const int q16 = 4 * cc + qq;
+        const int cl = cl0 + q16, c = u.cbase + cl;
+        if (rl < nrows && cl < ncols && (!u.tri || r >= c)) {
+          float vr[TC_S], vi[TC_S];
+#pragma unroll
+          for (int uu = 0; uu < TC_S; ++uu) {
+            vr[uu] = are[uu][qq];
+            vi[uu] = aim[uu][qq];
+          }
+          const int ecol = ec[(TC_CQ * cqt + q16) * y.es + y.eo];
+          const float sc = pow2f(er + ecol - 16);
+          df pr = combine7(vr), pi = combine7(vi);
+          pr.hi = __fmul_rn(pr.hi, sc);
+          pr.lo = __fmul_rn(pr.lo, sc);
+          pi.hi = __fmul_rn(pi.hi, sc);
+          pi.lo = __fmul_rn(pi.lo, sc);
+          zdf a = cv[q16];
+          a.re = df_sub(a.re, pr);
+          a.im = df_sub(a.im, pi);
+          C[r + u.ldc * c] = a;
         }
-        const int ecol = ec[(TU_CQ * cqt + qq) * y.es + y.eo];
-        const float sc = pow2f(er + ecol - 16);
-        df pr = combine7(vr), pi = combine7(vi);
-        pr.hi = __fmul_rn(pr.hi, sc);
-        pr.lo = __fmul_rn(pr.lo, sc);
-        pi.hi = __fmul_rn(pi.hi, sc);
-        pi.lo = __fmul_rn(pi.lo, sc);
-        zdf a = cv[qq];
-        a.re = df_sub(a.re, pr);
-        a.im = df_sub(a.im, pi);
-        C[r + u.ldc * c] = a;
       }
     }
-    // the accumulator set is read: the MMAs of block i + 2 may overwrite it
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
   }
   if (!ok) {
-    // let every copy and MMA still in flight finish (bounded waits) before
-    // the shared and tensor memory are released
-    if (tid == 0) {
-      for (int k = 0; k < 5; ++k)
-        while (wtd[k] < iss[k]) {
-          tc::mbar_wait(&bars[k], (uint32_t)(wtd[k] & 1), 200000000LL);
-          ++wtd[k];
-        }
-      atomicExch(&err[b], 1);
+    // let the copies and MMAs still in flight finish (bounded waits) before
+    // the shared and tensor memory are released: the row operand of the
+    // failed step's product, the failed step's MMAs and column copy, and the
+    // column copy issued for the step after it
+    if (tid == 0 && failed_i >= 0) {
+      const int fp = failed_i / ncbw;
+      tc::mbar_wait(&bars[0], (uint32_t)(fp & 1), 200000000LL);
+      tc::mbar_wait(&bars[3], (uint32_t)(failed_i & 1), 200000000LL);
+      tc::mbar_wait(&bars[1 + (failed_i & 1)], (uint32_t)((failed_i >> 1) & 1), 200000000LL);
+      const int nx = failed_i + 1;
+      if (nx < nblk) tc::mbar_wait(&bars[1 + (nx & 1)], (uint32_t)((nx >> 1) & 1), 200000000LL);
     }
+    if (tid == 0) atomicExch(&err[b], 1);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
@@ -744,7 +688,7 @@ cudaError_t prepare_her2k_tc() {
   const int dev = device_index();
   std::lock_guard<std::mutex> g(mu);
   if (dev >= 0 && done[dev]) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_cupd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TU_SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_cupd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_longk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, VX_SMEM);
   if (e == cudaSuccess && dev >= 0) done[dev] = true;
   return e;
@@ -816,8 +760,8 @@ cudaError_t her2k_tc(EigWork &w, int k0, int jb, cudaStream_t s) {
   u.y[1] = V;
   u.stall_b = take_stall(w, &u.stall_cycles);
   const int nrb = (mmax + 127) / 128;
-  const int nq = ((128 / TU_NB) * nrb + TU_CB - 1) / TU_CB;
-  PP_KT(KT_HER2K, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TU_SMEM, s>>>(u, w.nvec, w.tcErr)));
+  const int nq = (4 * nrb + TC_CB - 1) / TC_CB;
+  PP_KT(KT_HER2K, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>(u, w.nvec, w.tcErr)));
   count_launch(1);
   return cudaGetLastError();
 }
@@ -852,8 +796,8 @@ cudaError_t applyV_tc(EigWork &w, int k0, int jb, zdf *X, int64_t ldx, int64_t s
   u.x[1] = u.x[0];
   u.y[1] = u.y[0];
   const int nrb = (mmax + 127) / 128;
-  const int nq = ((ncols + TU_NB - 1) / TU_NB + TU_CB - 1) / TU_CB;
-  PP_KT(KT_APPLYV, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TU_SMEM, s>>>(u, w.nvec, w.tcErr)));
+  const int nq = ((ncols + 31) / 32 + TC_CB - 1) / TC_CB;
+  PP_KT(KT_APPLYV, s, (k_cupd_tc<<<dim3(nq, nrb, w.B), TC_NT, TC_SMEM, s>>>(u, w.nvec, w.tcErr)));
   count_launch(1);
   return cudaGetLastError();
 }
