@@ -188,6 +188,7 @@ def large_cell(nq):
         dn = float(torch.abs(D).sum(dim=0).max().item())
         del D
         checks.append({"q": qs[t].tolist(), "m": m, "info": int(res.info[t]),
+                       "nonfinite_columns": int((~torch.isfinite(Z.real) | ~torch.isfinite(Z.imag)).any(dim=0).sum()),
                        "residual": float((torch.linalg.vector_norm(DZ - Z * lam[None, :], dim=0).max() / dn).item()),
                        "orthogonality": float(torch.abs(Z.conj().T @ Z - torch.eye(m, dtype=Z.dtype, device=dev))
                                               .max().item()),
@@ -509,16 +510,19 @@ def other_configs(dev):
         pt = torch.tensor(phi, device=dev, requires_grad=True)
         target = spec.frequencies(q.detach(), pt.detach()) * torch.tensor(
             1.0 + 0.03 * rng.uniform(-1, 1, (len(q), c.n)), device=dev)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        w = spec.frequencies(q, pt)
-        loss = ((w - target) ** 2).sum()
-        loss.backward()
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
+        for rep in range(2):   # the first pass tunes the launch configuration of the backward's solve
+            q.grad = pt.grad = None
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            w = spec.frequencies(q, pt)
+            loss = ((w - target) ** 2).sum()
+            loss.backward()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
         res["4_n1588_forward_backward"] = {
             "workload": "N=1588, loss = sum (w - w_target)^2, dL/dq and dL/dPhi (autograd.Function, device tensors)",
             "sample": "8 of the 128 q", "value": len(q) / dt, "unit": "q-pts/s (forward + backward)", "s": dt,
+            "grad_phi_finite": bool(torch.isfinite(pt.grad).all()),
             "grad_phi_symmetric": bool(torch.allclose(pt.grad, pt.grad.T))}
     finally:
         spec.close()

@@ -948,21 +948,27 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
 // columns (k, k+1, k+2); l is the multiplier, piv marks a row interchange.
 // The factors and the working vector x live in scratch interleaved by thread
 // ([row][field][thread]) so that a warp's accesses coalesce; the finished
-// vector is written to its column of E once.
-constexpr int IV_F = 5;  // u0, u1, u2, l, x
+// vector is written to its column of E once.  Every pass over the rows runs
+// in chunks of IV_CH rows whose loads are all issued before the chunk's
+// arithmetic and stores: the recurrences are sequential in the row, and a
+// load behind a store to the same scratch array would otherwise wait out one
+// memory latency per row.  The arithmetic and its order are those of the
+// row-by-row loops.
+constexpr int IV_F = 5;   // u0, u1, u2, l, x
+constexpr int IV_CH = 8;  // rows per chunk
 template <class R>
-__global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee, int64_t sd, const int *nvec,
-                                              const double *ww, const int64_t *rng, const double *tinfo,
-                                              const int *cls, int64_t scl, const int *ncl, int cbase, C<R> *Eb,
-                                              int64_t lde, int64_t sE, double *scratch, uint8_t *pivb, int64_t T,
-                                              int64_t sS, int64_t sPv, int64_t *info) {
+__global__ void __launch_bounds__(64) k_invit(const double *__restrict__ dd, const double *__restrict__ ee, int64_t sd,
+                                              const int *nvec, const double *ww, const int64_t *rng,
+                                              const double *tinfo, const int *cls, int64_t scl, const int *ncl,
+                                              int cbase, C<R> *Eb, int64_t lde, int64_t sE, double *scratch,
+                                              uint8_t *pivb, int64_t T, int64_t sS, int64_t sPv, int64_t *info) {
   const int b = blockIdx.y;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = cbase + t;
   if (t >= T || c >= ncl[b]) return;
   const int n = nvec[b];
-  const double *d = dd + b * sd;
-  const double *e = ee + b * sd;
+  const double *__restrict__ d = dd + b * sd;
+  const double *__restrict__ e = ee + b * sd;
   const double *w = ww + b * sd;
   C<R> *E = Eb + b * sE;
   double *S = scratch + b * sS;
@@ -989,41 +995,52 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
     lam_prev = lam;
     // ---- factor T - lam I
     double p = d[0] - lam, qv = (n > 1) ? e[0] : 0.0;
-    for (int k = 0; k < n - 1; ++k) {
-      const double ck = e[k];
-      const double ak1 = d[k + 1] - lam;
-      const double bk1 = (k + 1 < n - 1) ? e[k + 1] : 0.0;
-      double u0, u1, u2, l, pn, qn, r0;
-      uint8_t sw;
-      // one FP64 division per row (FP64 is the scarce pipe): l from the
-      // pivot's reciprocal, and U is stored with 1/u0 so that the U solves
-      // multiply
-      if (fabs(p) >= fabs(ck)) {
-        r0 = (p == 0.0) ? 0.0 : 1.0 / p;
-        l = ck * r0;
-        u0 = p;
-        u1 = qv;
-        u2 = 0.0;
-        pn = ak1 - l * qv;
-        qn = bk1;
-        sw = 0;
-      } else {
-        r0 = 1.0 / ck;
-        l = p * r0;
-        u0 = ck;
-        u1 = ak1;
-        u2 = bk1;
-        pn = qv - l * ak1;
-        qn = -l * bk1;
-        sw = 1;
+    for (int kb = 0; kb < n - 1; kb += IV_CH) {
+      double ck[IV_CH], dk1[IV_CH], bk[IV_CH];
+#pragma unroll
+      for (int u = 0; u < IV_CH; ++u) {
+        const int k = kb + u;
+        ck[u] = k < n - 1 ? e[k] : 0.0;
+        dk1[u] = k < n - 1 ? d[k + 1] : 0.0;
+        bk[u] = k + 1 < n - 1 ? e[k + 1] : 0.0;
       }
-      SU0(k) = (fabs(u0) < pivtol) ? 1.0 / copysign(pivtol, u0) : r0;  // 1 / guarded pivot
-      SU1(k) = u1;
-      SU2(k) = u2;
-      SL(k) = l;
-      PIV(k) = sw;
-      p = pn;
-      qv = qn;
+#pragma unroll
+      for (int u = 0; u < IV_CH; ++u) {
+        const int k = kb + u;
+        if (k >= n - 1) break;
+        const double ak1 = dk1[u] - lam;
+        double u0, u1, u2, l, pn, qn, r0;
+        uint8_t sw;
+        // one FP64 division per row (FP64 is the scarce pipe): l from the
+        // pivot's reciprocal, and U is stored with 1/u0 so that the U solves
+        // multiply
+        if (fabs(p) >= fabs(ck[u])) {
+          r0 = (p == 0.0) ? 0.0 : 1.0 / p;
+          l = ck[u] * r0;
+          u0 = p;
+          u1 = qv;
+          u2 = 0.0;
+          pn = ak1 - l * qv;
+          qn = bk[u];
+          sw = 0;
+        } else {
+          r0 = 1.0 / ck[u];
+          l = p * r0;
+          u0 = ck[u];
+          u1 = ak1;
+          u2 = bk[u];
+          pn = qv - l * ak1;
+          qn = -l * bk[u];
+          sw = 1;
+        }
+        SU0(k) = (fabs(u0) < pivtol) ? 1.0 / copysign(pivtol, u0) : r0;  // 1 / guarded pivot
+        SU1(k) = u1;
+        SU2(k) = u2;
+        SL(k) = l;
+        PIV(k) = sw;
+        p = pn;
+        qv = qn;
+      }
     }
     SU0(n - 1) = 1.0 / ((fabs(p) < pivtol) ? copysign(pivtol, p) : p);
     SU1(n - 1) = 0.0;
@@ -1037,28 +1054,57 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
     }
     bool ok = true;
     for (int it = 0; it < iters && ok; ++it) {
-      // L solve with the recorded interchanges
+      // L solve with the recorded interchanges (x(k+1) of a chunk is read
+      // before x(k) is overwritten, as in the row-by-row loop)
       double xk = XS(0);
-      for (int k = 0; k < n - 1; ++k) {
-        const double xk1 = XS(k + 1);
-        const double l = SL(k);
-        if (PIV(k)) {
-          XS(k) = xk1;
-          xk = xk - l * xk1;
-        } else {
-          XS(k) = xk;
-          xk = xk1 - l * xk;
+      for (int kb = 0; kb < n - 1; kb += IV_CH) {
+        double x1[IV_CH], l[IV_CH];
+        uint8_t pv[IV_CH];
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u) {
+          const int k = kb + u;
+          const bool in = k < n - 1;
+          x1[u] = in ? XS(k + 1) : 0.0;
+          l[u] = in ? SL(k) : 0.0;
+          pv[u] = in ? PIV(k) : (uint8_t)0;
+        }
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u) {
+          const int k = kb + u;
+          if (k >= n - 1) break;
+          if (pv[u]) {
+            XS(k) = x1[u];
+            xk = xk - l[u] * x1[u];
+          } else {
+            XS(k) = xk;
+            xk = x1[u] - l[u] * xk;
+          }
         }
       }
       XS(n - 1) = xk;
       // U solve
       double y1 = 0.0, y2 = 0.0, amax = 0.0;
-      for (int k = n - 1; k >= 0; --k) {
-        const double y = (XS(k) - SU1(k) * y1 - SU2(k) * y2) * SU0(k);
-        XS(k) = y;
-        amax = fmax(amax, fabs(y));
-        y2 = y1;
-        y1 = y;
+      for (int kt = n - 1; kt >= 0; kt -= IV_CH) {
+        double xv[IV_CH], a0[IV_CH], a1[IV_CH], a2[IV_CH];
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u) {
+          const int k = kt - u;
+          const bool in = k >= 0;
+          xv[u] = in ? XS(k) : 0.0;
+          a0[u] = in ? SU0(k) : 0.0;
+          a1[u] = in ? SU1(k) : 0.0;
+          a2[u] = in ? SU2(k) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u) {
+          const int k = kt - u;
+          if (k < 0) break;
+          const double y = (xv[u] - a1[u] * y1 - a2[u] * y2) * a0[u];
+          XS(k) = y;
+          amax = fmax(amax, fabs(y));
+          y2 = y1;
+          y1 = y;
+        }
       }
       if (!(amax > 0.0) || !isfinite(amax)) {
         ok = false;
@@ -1069,35 +1115,87 @@ __global__ void __launch_bounds__(64) k_invit(const double *dd, const double *ee
       for (int pass = 0; pass < 2 && j > j0; ++pass) {
         for (int jp = j0; jp < j; ++jp) {
           double dot = 0.0;
-          for (int k = 0; k < n; ++k) dot += RT<R>::to(E[k + lde * jp].re) * XS(k);
-          for (int k = 0; k < n; ++k) XS(k) = XS(k) - dot * RT<R>::to(E[k + lde * jp].re);
+          for (int kb = 0; kb < n; kb += IV_CH) {
+            double ev[IV_CH], xv[IV_CH];
+#pragma unroll
+            for (int u = 0; u < IV_CH; ++u) {
+              const int k = kb + u;
+              const bool in = k < n;
+              ev[u] = in ? RT<R>::to(E[k + lde * jp].re) : 0.0;
+              xv[u] = in ? XS(k) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < IV_CH; ++u)
+              if (kb + u < n) dot += ev[u] * xv[u];
+          }
+          for (int kb = 0; kb < n; kb += IV_CH) {
+            double ev[IV_CH], xv[IV_CH];
+#pragma unroll
+            for (int u = 0; u < IV_CH; ++u) {
+              const int k = kb + u;
+              const bool in = k < n;
+              ev[u] = in ? RT<R>::to(E[k + lde * jp].re) : 0.0;
+              xv[u] = in ? XS(k) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < IV_CH; ++u)
+              if (kb + u < n) XS(kb + u) = xv[u] - dot * ev[u];
+          }
         }
       }
       double nrm2 = 0.0;
-      for (int k = 0; k < n; ++k) {
-        const double v = XS(k) * inv;
-        nrm2 += v * v;
+      for (int kb = 0; kb < n; kb += IV_CH) {
+        double xv[IV_CH];
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u) xv[u] = kb + u < n ? XS(kb + u) : 0.0;
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u) {
+          if (kb + u < n) {
+            const double v = xv[u] * inv;
+            nrm2 += v * v;
+          }
+        }
       }
       if (!(nrm2 > 1e-280)) {
         ok = false;
         break;
       }
       const double sc = inv / sqrt(nrm2);
-      for (int k = 0; k < n; ++k) XS(k) = XS(k) * sc;
+      for (int kb = 0; kb < n; kb += IV_CH) {
+        double xv[IV_CH];
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u) xv[u] = kb + u < n ? XS(kb + u) : 0.0;
+#pragma unroll
+        for (int u = 0; u < IV_CH; ++u)
+          if (kb + u < n) XS(kb + u) = xv[u] * sc;
+      }
     }
     if (!ok) bad = 1;
     // sign convention of dstein: the largest component is positive
     double big = -1.0;
-    int kb = 0;
-    for (int k = 0; k < n; ++k) {
-      const double v = fabs(XS(k));
-      if (v > big) {
-        big = v;
-        kb = k;
+    int kbig = 0;
+    for (int kb = 0; kb < n; kb += IV_CH) {
+      double xv[IV_CH];
+#pragma unroll
+      for (int u = 0; u < IV_CH; ++u) xv[u] = kb + u < n ? XS(kb + u) : 0.0;
+#pragma unroll
+      for (int u = 0; u < IV_CH; ++u) {
+        const double v = fabs(xv[u]);
+        if (kb + u < n && v > big) {
+          big = v;
+          kbig = kb + u;
+        }
       }
     }
-    const double sgn = XS(kb) < 0.0 ? -1.0 : 1.0;
-    for (int k = 0; k < n; ++k) E[k + lde * j] = cfrom64<R>(XS(k) * sgn, 0.0);
+    const double sgn = XS(kbig) < 0.0 ? -1.0 : 1.0;
+    for (int kb = 0; kb < n; kb += IV_CH) {
+      double xv[IV_CH];
+#pragma unroll
+      for (int u = 0; u < IV_CH; ++u) xv[u] = kb + u < n ? XS(kb + u) : 0.0;
+#pragma unroll
+      for (int u = 0; u < IV_CH; ++u)
+        if (kb + u < n) E[kb + u + lde * j] = cfrom64<R>(xv[u] * sgn, 0.0);
+    }
   }
   if (bad) atomicOr((unsigned long long *)&info[b], (unsigned long long)PP_INFO_NOORTH);
 #undef SU0

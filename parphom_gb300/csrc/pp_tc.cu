@@ -439,7 +439,18 @@ __device__ __forceinline__ int slice_kstep(const zdf *strow, bool neg_im, uint8_
   if (NKS == 4) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 2));
   int E = 0;
   if (amax > 0.f) frexpf(amax, &E);
-  const float sc = (part && neg_im) ? -pow2f(-E) : pow2f(-E);
+  // 2^-E exceeds the float range when the largest magnitude is subnormal
+  // (E <= -128, e.g. the far tail of a localised eigenvector): such rows are
+  // scaled in two exact power-of-two steps
+  const int e1 = E < -100 ? 100 : 0;
+  const float sc = (part && neg_im) ? -pow2f(-E - e1) : pow2f(-E - e1);
+  if (e1) {
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      th[t] = __fmul_rn(th[t], 0x1p100f);
+      tl[t] = __fmul_rn(tl[t], 0x1p100f);
+    }
+  }
 #pragma unroll
   for (int t = 0; t < 16; ++t) {
     th[t] = __fmul_rn(th[t], sc);

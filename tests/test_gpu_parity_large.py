@@ -82,3 +82,32 @@ def test_n1588_frequencies_and_velocities(n1588, prec):
     S, ctx, qs, refs = n1588
     res = ctx.solve(qs, api.EigOpts(jobz="N", vel=True, vel_method="A", precision=prec), want_z=False)
     print(prec, _check(S, qs, refs, res, vectors=False))
+
+
+def test_n1588_vectors_with_subnormal_tails():
+    """Band-path q-points 64 and 80 at N=1588 have eigenvectors whose far
+    components fall below the single-precision normal range at some stage
+    of the back-transform; the tensor-core long-K slicing scales such row
+    chunks in two exact steps.  Every column must be finite and the pairs
+    must keep their residual and orthogonality (mixed form, full vectors)."""
+    import torch
+    c, phi = _cell(11)
+    ctx = api.PhononContext.from_cell(c, phi)
+    try:
+        qs = synth.band_path(128)[[64, 80]]
+        res = ctx.solve(qs, api.EigOpts(jobz="V", precision=api.PP_PREC_MIXED))
+        dev = torch.device("cuda")
+        cw = float(np.float32(15.633302)) * float(np.float32(33.35641))
+        for t in range(len(qs)):
+            n = ctx.n
+            assert res.m[t] == n and res.info[t] == 0
+            Z = torch.as_tensor(res.z[t][:, :n], device=dev)
+            assert bool(torch.isfinite(Z.real).all()) and bool(torch.isfinite(Z.imag).all())
+            D = torch.as_tensor(ctx.dynamical_matrix(qs[t]), device=dev)
+            lam = torch.as_tensor(np.sign(res.w[t, :n]) * (res.w[t, :n] / cw) ** 2, device=dev)
+            dn = float(torch.abs(D).sum(dim=0).max())
+            resid = float((torch.linalg.vector_norm(D @ Z - Z * lam[None, :], dim=0).max() / dn))
+            orth = float(torch.abs(Z.conj().T @ Z - torch.eye(n, dtype=Z.dtype, device=dev)).max())
+            assert resid < 1e-11 and orth < 1e-10, (resid, orth)
+    finally:
+        ctx.close()
