@@ -269,8 +269,9 @@ int ensure_ws_sized(pp_ctx *c, int B, int mcap, int64_t n, int64_t nbnd_max, int
   add((void **)&w.scratch, 8 * (size_t)B * 5 * n * T);
   add((void **)&w.piv, (size_t)B * n * T);
   add((void **)&w.info, 8 * (size_t)B);
-  add((void **)&w.Tf, 16 * (size_t)B * 1024);
-  add((void **)&w.G, 16 * (size_t)B * 1024);
+  const int64_t npan = std::max<int64_t>(1, (n - 1 + nb - 1) / nb);
+  w.sTfp = (int64_t)B * 1024;
+  add((void **)&w.Tf, 16 * (size_t)npan * B * 1024);
   add(&w.Wb, 16 * (size_t)B * 32 * ldwp);
   add(&w.Wp, 16 * (size_t)B * ksplit * 32 * ldwp);
   w.nbr = nbr;
@@ -368,8 +369,7 @@ EigWork view_of(const EigWork &w, int off, int cnt) {
   v.scratch = (double *)sh(w.scratch, 8 * 5 * nmax * (size_t)T);
   v.piv = (uint8_t *)sh(w.piv, nmax * (size_t)T);
   v.info = (int64_t *)sh(w.info, 8);
-  v.Tf = (z64 *)sh(w.Tf, 16 * 1024);
-  v.G = (z64 *)sh(w.G, 16 * 1024);
+  v.Tf = (z64 *)sh(w.Tf, 16 * 1024);  // panel stride sTfp unchanged
   v.Wb = sh(w.Wb, 16 * 32 * (size_t)w.ldwp);
   v.Wp = sh(w.Wp, 16 * (size_t)w.ksplit * 32 * w.ldwp);
   v.Xr = sh(w.Xr, 16 * (size_t)w.lda * std::max(w.nbr, 1));

@@ -298,12 +298,16 @@ __global__ void __launch_bounds__(HL_NT, HL_BPS) k_hemv_lower(const C<R> *Ab, in
     int Rt, Ct;
     tile_pair(p, Rt, Ct);
     const int rt0 = r0 + Rt * HL_T, ct0 = r0 + Ct * HL_T;
+    // element (r, c) = (tid % HL_T, tid / HL_T + CS j), j < HL_T / CS
+    constexpr int CS = HL_NT / HL_T;
+    const int r = tid % HL_T, cb = tid / HL_T;
+    const int rr = rt0 + r;
+    const C<R> *src = A + rr + lda * (ct0 + cb);
+    C<R> *dst = &tile[buf][cb * HL_LD + r];
 #pragma unroll
-    for (int e = tid; e < HL_T * HL_T; e += HL_NT) {
-      const int c = e / HL_T, r = e % HL_T;
-      const int rr = rt0 + r, cc = ct0 + c;
-      const bool ok = rr < n && cc < n;
-      cp_async16(&tile[buf][c * HL_LD + r], ok ? (const void *)&A[rr + lda * cc] : (const void *)A, ok);
+    for (int j = 0; j < HL_T / CS; ++j) {
+      const bool ok = rr < n && ct0 + cb + CS * j < n;
+      cp_async16(dst + CS * j * HL_LD, ok ? (const void *)(src + CS * j * lda) : (const void *)A, ok);
     }
     if (tid < HL_T) {
       const int rr = rt0 + tid;
@@ -1217,8 +1221,9 @@ cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
   const int64_t sPv = (int64_t)w.nmax * T;
   for (int64_t cb = 0; cb < w.mcap; cb += T) {
     dim3 g(cdiv(T, 64), w.B);
-    PP_KT(KT_INVIT, s, (k_invit<R><<<g, 64, 0, s>>>(w.d, w.e, sd, w.nvec, w.w, w.rng, w.tinfo, w.cls, scl, w.ncl, (int)cb, (C<R> *)w.E,
-                                w.lde, w.sE, w.scratch, w.piv, T, sS, sPv, w.info)));
+    PP_KT(KT_INVIT, s, (k_invit<R><<<g, 64, 0, s>>>(w.d, w.e, sd, w.nvec, w.w, w.rng, w.tinfo, w.cls, scl, w.ncl,
+                                                    (int)cb, (C<R> *)w.E, w.lde, w.sE, w.scratch, w.piv, T, sS, sPv,
+                                                    w.info)));
     count_launch(1);
   }
   k_clusters<<<w.B, 32, 0, s>>>(w.w, sd, w.rng, w.tinfo, w.cls, scl, w.ncl, 1e-5);
@@ -1233,27 +1238,26 @@ cudaError_t tridiag_eigenvectors(EigWork &w, cudaStream_t s) {
 constexpr int BT_J = 64;     // columns per block
 constexpr int BT_RK = 16;    // rows per k-step
 constexpr int BT_RCH = 512;  // rows per split-K chunk
-constexpr int GRAM_RCH = 64; // rows per chunk of the Gram product V^H V
 
 // Wp[ks][a][j] = sum_{r in chunk ks} conj(V(r,a)) X(r,j) for a < jb.
-// V(r,a) = A(r, k0+a) for r >= k0+a+1 (zero above).  X is E (ncol = m of
-// the matrix) or, with x_is_v, the panel V itself (ncol = jb, same mask).
+// V(r,a) = A(r, k0+a) for r >= k0+a+1 (zero above); j < the matrix's m, or
+// ncol_fixed.
 template <class R>
 __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_t sA, const C<R> *Xb, int64_t ldx,
-                                             int64_t sX, int x_is_v, const int *nvec, const int64_t *rng, int k0,
-                                             int jb, C<R> *Wp, int64_t ldwp, int64_t sWp, int ncol_fixed, int rch) {
+                                             int64_t sX, const int *nvec, const int64_t *rng, int k0, int jb,
+                                             C<R> *Wp, int64_t ldwp, int64_t sWp, int ncol_fixed, int rch) {
   __shared__ C<R> sV[BT_RK][32];
   __shared__ C<R> sXt[BT_RK][BT_J];
   const int b = blockIdx.z;
   const int n = nvec[b];
-  const int ncol = x_is_v ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
+  const int ncol = ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2];
   const int j0 = blockIdx.x * BT_J;
   const int ks = blockIdx.y;
   const int rbeg = k0 + 1 + ks * rch;
   if (j0 >= ncol || rbeg >= n) return;
   const C<R> *A = Ab + b * sA;
-  const C<R> *X = x_is_v ? (A + lda * k0) : (Xb + b * sX);
-  const int64_t ldX = x_is_v ? lda : ldx;
+  const C<R> *X = Xb + b * sX;
+  const int64_t ldX = ldx;
   const int tj = threadIdx.x & 63, ta = threadIdx.x >> 6;
   C<R> acc[8];
 #pragma unroll
@@ -1268,8 +1272,7 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
     for (int e = threadIdx.x; e < BT_RK * BT_J; e += 256) {
       const int jx = e & 63, rr = e >> 6;
       const int r = r0 + rr, j = j0 + jx;
-      bool ok = r < rend && j < ncol;
-      if (x_is_v) ok = ok && r >= k0 + j + 1;
+      const bool ok = r < rend && j < ncol;
       sXt[rr][jx] = ok ? X[r + ldX * j] : cz<R>();
     }
     __syncthreads();
@@ -1291,90 +1294,121 @@ __global__ void __launch_bounds__(256) k_vhx(const C<R> *Ab, int64_t lda, int64_
   }
 }
 
-// Sum the split-K partials.  mode 0: G = V^H V (z64, 32x32).  mode 1:
-// Y = Tf * (V^H E), Tf upper triangular, written to Wb.
+// Sum the split-K partials of V^H X and apply the panel's compact-WY factor
+// (Tf at Tf + 1024 b, upper triangular): mode 1 Y = Tf (V^H X), mode 2
+// Y = Tf^H (V^H X); written to Wb.
+// Block of BR_NT threads = 32 columns j x 8 groups of panel rows a (a = g,
+// g + 8, g + 16, g + 24): the partials are summed into shared memory, then
+// every thread forms its four rows of the product with Tf.
+constexpr int BR_NT = 256;
 template <class R>
-__global__ void __launch_bounds__(64) k_btred(const C<R> *Wp, int64_t ldwp, int64_t sWp, const int *nvec,
-                                              const int64_t *rng, int k0, int jb, int mode, z64 *G, const z64 *Tf,
-                                              C<R> *Wb, int64_t sWb, int ncol_fixed, int nks_fixed = 0) {
-  __shared__ C<R> col[32][64];
-  __shared__ z64 sT[32][32];
+__global__ void __launch_bounds__(BR_NT) k_btred(const C<R> *Wp, int64_t ldwp, int64_t sWp, const int *nvec,
+                                                 const int64_t *rng, int k0, int jb, int mode, const z64 *Tf,
+                                                 C<R> *Wb, int64_t sWb, int ncol_fixed, int nks_fixed = 0) {
+  __shared__ C<R> col[32][33];
+  __shared__ z64 sT[32][33];
   const int b = blockIdx.y;
   const int n = nvec[b];
-  const int ncol = mode == 0 ? jb : (ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2]);
+  const int ncol = ncol_fixed > 0 ? ncol_fixed : (int)rng[b * 8 + 2];
   // split-K partials to sum: one per BT_RCH rows, or nks_fixed
   const int nks = nks_fixed > 0 ? (n - k0 - 1 > 0 ? nks_fixed : 0) : (n - k0 - 1 + BT_RCH - 1) / BT_RCH;
-  if (mode != 0) {
-    for (int e = threadIdx.x; e < 32 * 32; e += 64) sT[e / 32][e % 32] = Tf[b * 1024 + e];
+  const int j0 = blockIdx.x * 32;
+  if (j0 >= ncol || nks <= 0) return;
+  for (int e = threadIdx.x; e < 32 * 32; e += BR_NT) sT[e / 32][e % 32] = Tf[b * 1024 + e];
+  const int jl = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int j = j0 + jl;
+  for (int a = g; a < jb; a += 8) {
+    C<R> s = cz<R>();
+    if (j < ncol)
+      for (int ks = 0; ks < nks; ++ks) s = cadd(s, Wp[b * sWp + ((int64_t)ks * 32 + a) * ldwp + j]);
+    col[a][jl] = s;
   }
   __syncthreads();
-  const int j = blockIdx.x * 64 + threadIdx.x;
-  if (j >= ncol || nks <= 0) return;
-  for (int a = 0; a < jb; ++a) {
-    C<R> s = cz<R>();
-    for (int ks = 0; ks < nks; ++ks) s = cadd(s, Wp[b * sWp + ((int64_t)ks * 32 + a) * ldwp + j]);
-    col[a][threadIdx.x] = s;
-  }
-  if (mode == 0) {
-    for (int a = 0; a < jb; ++a) G[b * 1024 + a * 32 + j] = cto64(col[a][threadIdx.x]);
-    return;
-  }
-  for (int a = 0; a < jb; ++a) {
+  if (j >= ncol) return;
+  for (int a = g; a < jb; a += 8) {
     C<R> acc = cz<R>();
     if (mode == 1) {
-      for (int a2 = a; a2 < jb; ++a2) cmac(acc, cfrom64<R>(sT[a][a2]), col[a2][threadIdx.x]);
+      for (int a2 = a; a2 < jb; ++a2) cmac(acc, cfrom64<R>(sT[a][a2]), col[a2][jl]);
     } else {  // mode 2: Tf^H (lower triangular)
-      for (int a2 = 0; a2 <= a; ++a2) cmac(acc, cfrom64<R>(zconj(sT[a2][a])), col[a2][threadIdx.x]);
+      for (int a2 = 0; a2 <= a; ++a2) cmac(acc, cfrom64<R>(zconj(sT[a2][a])), col[a2][jl]);
     }
     Wb[b * sWb + (int64_t)a * ldwp + j] = cfin(acc);
   }
 }
 
-// G = V^H V from the Gram partials of k_vhx (row chunks of GRAM_RCH, stored
-// 32 x 32 per chunk): one thread per entry.
+// Compact-WY factors of every panel in one launch, one block per (panel,
+// matrix): the Gram matrix G = V^H V of the panel's Householder vectors
+// (products in the arithmetic R, rows staged WY_RK at a time and the sums
+// renormalised after each stage, each thread four entries), then Tf by
+// zlarft's forward columnwise recurrence in FP64: Tf(a,a) = tau_a,
+// Tf(0:a, a) = -tau_a Tf(0:a, 0:a) G(0:a, a).  Tf of panel P for matrix b
+// goes to Tf + P sTfp + 1024 b (row-major 32 x 32).  Panel widths follow the
+// batch's largest order (nref = nmax - 1); reflectors past a matrix's own
+// order have tau = 0 and give zero columns of Tf.
+constexpr int WY_RK = 16;
 template <class R>
-__global__ void __launch_bounds__(1024) k_gram_sum(const C<R> *Wp, int64_t sWp, const int *nvec, int k0, z64 *G) {
-  const int b = blockIdx.x;
+__global__ void __launch_bounds__(256) k_wy_factors(const C<R> *Ab, int64_t lda, int64_t sA, const int *nvec,
+                                                     const z64 *tau, int64_t sd, int nb, int nref, z64 *Tf,
+                                                     int64_t sTfp) {
+  __shared__ C<R> sV[WY_RK][33];
+  __shared__ z64 G[32][33];
+  __shared__ z64 sT[32][33];
+  const int P = blockIdx.x, b = blockIdx.y;
   const int n = nvec[b];
-  const int a = threadIdx.x >> 5, j = threadIdx.x & 31;
-  const int nks = (n - k0 - 1 + GRAM_RCH - 1) / GRAM_RCH;
-  C<R> s = cz<R>();
-  for (int ks = 0; ks < nks; ++ks) s = cadd(s, Wp[b * sWp + ((int64_t)ks * 32 + a) * 32 + j]);
-  G[b * 1024 + a * 32 + j] = cto64(s);
-}
-
-// Tf (zlarft, forward, columnwise): Tf(a,a) = tau_a,
-// Tf(0:a, a) = -tau_a Tf(0:a, 0:a) G(0:a, a).
-__global__ void k_buildT(const z64 *G, const z64 *tau, int64_t sd, const int *nvec, int k0, int jb, z64 *Tf) {
-  __shared__ z64 sT[32][32];
-  __shared__ z64 tmp[32];
-  const int b = blockIdx.x;
-  const int n = nvec[b];
-  const int a = threadIdx.x;
-  for (int e = a; e < 1024; e += 32) sT[e / 32][e % 32] = z64{0.0, 0.0};
-  __syncthreads();
-  for (int jj = 0; jj < jb; ++jj) {
-    const int i = k0 + jj;
-    const z64 tj = (i < n - 1) ? tau[b * sd + i] : z64{0.0, 0.0};
-    if (a < jj) {
-      z64 acc{0.0, 0.0};
-      for (int a2 = a; a2 < jj; ++a2) {
-        const z64 g = G[b * 1024 + a2 * 32 + jj];
-        const z64 tt = sT[a][a2];
-        acc.re += tt.re * g.re - tt.im * g.im;
-        acc.im += tt.re * g.im + tt.im * g.re;
-      }
-      tmp[a] = acc;
+  const int k0 = P * nb;
+  const int jb = min(nb, nref - k0);
+  const C<R> *A = Ab + b * sA;
+  const int tid = threadIdx.x;
+  const int ga = tid >> 3, gj = (tid & 7) * 4;  // G(ga, gj .. gj+3)
+  C<R> acc[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q] = cz<R>();
+  for (int r0 = k0 + 1; r0 < n; r0 += WY_RK) {
+    for (int e = tid; e < WY_RK * 32; e += 256) {
+      const int a = e & 31, rr = e >> 5, r = r0 + rr;
+      sV[rr][a] = (a < jb && r < n && r >= k0 + a + 1) ? A[r + lda * (k0 + a)] : cz<R>();
     }
     __syncthreads();
-    if (a < jj) {
-      const z64 v = zmul(tj, tmp[a]);
-      sT[a][jj] = z64{-v.re, -v.im};
+#pragma unroll 4
+    for (int rr = 0; rr < WY_RK; ++rr) {
+      const C<R> va = sV[rr][ga];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) cmacc(acc[q], va, sV[rr][gj + q]);
     }
-    if (a == jj) sT[jj][jj] = tj;
+    // renormalise after every WY_RK rows: the unnormalised low word of the
+    // multiply-add is meant for short sums, the panel runs over all n rows
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] = cfin(acc[q]);
     __syncthreads();
   }
-  for (int e = a; e < 1024; e += 32) Tf[b * 1024 + e] = sT[e / 32][e % 32];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) G[ga][gj + q] = cto64(cfin(acc[q]));
+  for (int e = tid; e < 1024; e += 256) sT[e / 32][e % 32] = z64{0.0, 0.0};
+  __syncthreads();
+  if (tid < 32) {
+    const int a = tid;
+    for (int jj = 0; jj < jb; ++jj) {
+      const int i = k0 + jj;
+      const z64 tj = (i < n - 1) ? tau[b * sd + i] : z64{0.0, 0.0};
+      z64 acc2{0.0, 0.0};
+      for (int a2 = a; a2 < jj; ++a2) {
+        const z64 g = G[a2][jj];
+        const z64 tt = sT[a][a2];
+        acc2.re += tt.re * g.re - tt.im * g.im;
+        acc2.im += tt.re * g.im + tt.im * g.re;
+      }
+      __syncwarp();
+      if (a < jj) {
+        const z64 v = zmul(tj, acc2);
+        sT[a][jj] = z64{-v.re, -v.im};
+      }
+      if (a == jj) sT[jj][jj] = tj;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  z64 *T = Tf + (int64_t)P * sTfp + (int64_t)b * 1024;
+  for (int e = tid; e < 1024; e += 256) T[e] = sT[e / 32][e % 32];
 }
 
 // E(r, j) -= sum_a V(r, a) Y(a, j), r in [k0+1, n), j < m.
@@ -1448,30 +1482,30 @@ cudaError_t back_transform(EigWork &w, cudaStream_t s) {
   C<R> *E = (C<R> *)w.E;
   C<R> *Wp = (C<R> *)w.Wp;
   C<R> *Wb = (C<R> *)w.Wb;
+  // compact-WY factors of all panels
+  PP_KT(KT_BTRED, s, (k_wy_factors<R><<<dim3(cdiv(nref, nb), B), 256, 0, s>>>(A, w.lda, w.sA, w.nvec, w.tau, sd, nb,
+                                                                           nref, w.Tf, w.sTfp)));
+  count_launch(1);
   const int kstart = ((nref - 1) / nb) * nb;
   for (int k0 = kstart; k0 >= 0; k0 -= nb) {
     const int jb = min(nb, nref - k0);
     const int ks = cdiv(nmax - k0 - 1, BT_RCH);
-    const int ksg = cdiv(nmax - k0 - 1, GRAM_RCH);
-    // Tf from G = V^H V
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb, Wp, 32, sWp, 0, GRAM_RCH)));
-    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
-    k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
+    const z64 *Tf = w.Tf + (int64_t)(k0 / nb) * w.sTfp;
     // Y = Tf V^H E ; E -= V Y (on the tensor cores in the double-float form,
     // over all mcap columns)
     const bool tc = std::is_same<R, df>::value && w.tcS && tc_enabled();
     if (tc) {
       PP_CUDA_TRY(vhx_tc(w, k0, jb, (const zdf *)E, w.lde, w.sE, w.mcap, (zdf *)Wp, ldwp, sWp, s));
-      PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, w.mcap, vhx_tc_splits(w))));
+      PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 32), B), BR_NT, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, Tf, Wb, sWb, w.mcap, vhx_tc_splits(w))));
       PP_CUDA_TRY(applyV_tc(w, k0, jb, (zdf *)E, w.lde, w.sE, (const zdf *)Wb, ldwp, sWb, w.mcap, s));
-      count_launch(4);
+      count_launch(1);
     } else {
-      PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, 0, w.nvec, w.rng, k0,
+      PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(w.mcap, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, E, w.lde, w.sE, w.nvec, w.rng, k0,
                                                                jb, Wp, ldwp, sWp, 0, BT_RCH)));
-      PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, w.G, w.Tf, Wb, sWb, 0)));
+      PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(w.mcap, 32), B), BR_NT, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 1, Tf, Wb, sWb, 0)));
       PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(w.mcap, AV_T), B), 256, 0, s>>>(
           A, w.lda, w.sA, Wb, ldwp, sWb, E, w.lde, w.sE, w.nvec, w.rng, k0, jb, 0)));
-      count_launch(6);
+      count_launch(3);
     }
   }
   return cudaGetLastError();
@@ -1563,24 +1597,23 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
   count_launch(1);
   // X <- Q^H X = Q_last^H ... Q_0^H X: panels in forward order, Tf^H
   const int nref = nmax - 1;
+  PP_KT(KT_BTRED, s, (k_wy_factors<R><<<dim3(cdiv(nref, nb), B), 256, 0, s>>>(A, w.lda, w.sA, w.nvec, w.tau, sd, nb,
+                                                                           nref, w.Tf, w.sTfp)));
+  count_launch(1);
   for (int k0 = 0; k0 < nref; k0 += nb) {
     const int jb = min(nb, nref - k0);
     const int ks = cdiv(nmax - k0 - 1, BT_RCH);
-    const int ksg = cdiv(nmax - k0 - 1, GRAM_RCH);
-    PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(1, ksg, B), 256, 0, s>>>(A, w.lda, w.sA, A, w.lda, w.sA, 1, w.nvec, w.rng, k0, jb,
-                                                             Wp, 32, sWp, 0, GRAM_RCH)));
-    PP_KT(KT_BTRED, s, (k_gram_sum<R><<<B, 1024, 0, s>>>(Wp, sWp, w.nvec, k0, w.G)));
-    k_buildT<<<B, 32, 0, s>>>(w.G, w.tau, sd, w.nvec, k0, jb, w.Tf);
+    const z64 *Tf = w.Tf + (int64_t)(k0 / nb) * w.sTfp;
     const bool tc = std::is_same<R, df>::value && w.tcS && tc_enabled();
     if (tc) {
       PP_CUDA_TRY(vhx_tc(w, k0, jb, (const zdf *)X, ldx, sX, nrows, (zdf *)Wp, ldwp, sWp, s));
     } else {
-      PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(nrows, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, X, ldx, sX, 0, w.nvec,
+      PP_KT(KT_VHX, s, (k_vhx<R><<<dim3(cdiv(nrows, BT_J), ks, B), 256, 0, s>>>(A, w.lda, w.sA, X, ldx, sX, w.nvec,
                                                                                w.rng, k0, jb, Wp, ldwp, sWp, nrows,
                                                                                BT_RCH)));
     }
-    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(nrows, 64), B), 64, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 2,
-                                                                          w.G, w.Tf, Wb, sWb, nrows,
+    PP_KT(KT_BTRED, s, (k_btred<R><<<dim3(cdiv(nrows, 32), B), BR_NT, 0, s>>>(Wp, ldwp, sWp, w.nvec, w.rng, k0, jb, 2,
+                                                                          Tf, Wb, sWb, nrows,
                                                                           tc ? vhx_tc_splits(w) : 0)));
     if (tc) {
       PP_CUDA_TRY(applyV_tc(w, k0, jb, (zdf *)X, ldx, sX, (const zdf *)Wb, ldwp, sWb, nrows, s));
@@ -1588,7 +1621,7 @@ cudaError_t back_transform_rows(EigWork &w, const int *d_rows, int nrows, cudaSt
       PP_KT(KT_APPLYV, s, (k_applyV<R><<<dim3(cdiv(nmax - k0 - 1, AV_T), cdiv(nrows, AV_T), B), 256, 0, s>>>(
                               A, w.lda, w.sA, Wb, ldwp, sWb, X, ldx, sX, w.nvec, w.rng, k0, jb, nrows)));
     }
-    count_launch(6);
+    count_launch(tc ? 1 : 3);  // the tensor-core helpers count their own launches
   }
   // Eb = X^H Z
   if (std::is_same<R, df>::value && w.tcS && tc_enabled()) {

@@ -78,8 +78,8 @@ struct EigWork {
   int64_t *info = nullptr;   // [B] info bits
 
   // back-transform
-  z64 *Tf = nullptr;      // [B][32*32] compact-WY factor of one panel
-  z64 *G = nullptr;       // [B][32*32] Gram matrix V^H V of one panel
+  z64 *Tf = nullptr;      // [npanels][B][32*32] compact-WY factors of all panels
+  int64_t sTfp = 0;       // panel stride of Tf (the full batch's B * 1024)
   void *Wb = nullptr;     // [B][32*ldwp]     T V^H E
   void *Wp = nullptr;     // [B][ksplit][32*ldwp] split-K partials
   int ksplit = 0;
