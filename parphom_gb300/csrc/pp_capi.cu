@@ -118,7 +118,7 @@ struct pp_ctx {
   int64_t *d_m = nullptr, *d_nz = nullptr, *d_info = nullptr;
   // extra streams for the other parts of a batch (forked from and joined to
   // the working stream with events, so that they are captured into the graph)
-  static constexpr int MAX_SPLIT = 16;
+  static constexpr int MAX_SPLIT = 32;
   cudaStream_t aux[MAX_SPLIT - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[MAX_SPLIT - 1] = {};
   // launch configuration of the current batch (autotuned or from the switches)
@@ -576,9 +576,9 @@ int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_
     const bool can_tune = graphs_enabled() && !pp::kt_mask && !tc_stall_armed() && cs == cudaStreamCaptureStatusNone;
     if (t.split < 0 && !can_tune) t = Tuned{split_ways(), 6, 0.f};
     if (t.split < 0) {
-      // greedy: split over {4, 8, 16} (at most B), then 4 instead of 6 mat-vec blocks per SM
+      // greedy: split over {4, 8, 16, 32} (at most B), then 4 instead of 6 mat-vec blocks per SM
       Tuned best{std::min(B, 8), 6, 1e30f};
-      for (int sp : {4, 8, 16}) {
+      for (int sp : {4, 8, 16, 32}) {
         if (sp > B && sp != 4) continue;
         const int spc = std::min(sp, B);
         const float ms = time_config(c, B, o, mcap, want_z, spc, 6);

@@ -51,9 +51,13 @@ def _digits_twosum(hi, lo, E):
 
 
 def _digits_fixed_grid(hi, lo, E):
-    sc = np.ldexp(np.ones_like(E, dtype=np.float64), -E).astype(f32)
-    th = (hi * sc).astype(f32)
-    tl = (lo * sc).astype(f32)
+    # rows whose largest magnitude is subnormal (E <= -128) scale in two exact
+    # steps, 2^100 first: 2^-E alone overflows float32
+    e1 = np.where(E < -100, 100, 0)
+    pre = np.ldexp(np.ones_like(E, dtype=np.float64), e1).astype(f32)
+    sc = np.ldexp(np.ones_like(E, dtype=np.float64), -E - e1).astype(f32)
+    th = ((hi * pre).astype(f32) * sc).astype(f32)
+    tl = ((lo * pre).astype(f32) * sc).astype(f32)
     out = []
     for s in range(7):
         mag = f32(1.5 * 2.0 ** (15 - 8 * s))
@@ -94,3 +98,25 @@ def test_slice_products_accumulate_exactly_in_fp32():
         for t in range(7 - s):
             p = d[s][:, None, :].astype(np.float64) * d[t][None, :, :].astype(np.float64)
             assert np.abs(p).sum(axis=2).max() < 2.0 ** 24
+
+
+def test_subnormal_rows_slice_finite_and_exact():
+    """Rows whose largest value is below the float32 normal range (the far
+    tail of a localised eigenvector): the two-step scale keeps every digit
+    finite and equal to the per-element TwoSum digits (which scale with
+    ldexp), and the digits reconstruct the row."""
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal((200, 64)) * 10.0 ** rng.uniform(-43, -40, (200, 1))
+    hi = x.astype(f32)
+    lo = np.zeros_like(hi)
+    amax = np.abs(hi).max(axis=1)
+    assert np.all(amax < np.finfo(f32).tiny)
+    _, E = np.frexp(amax.astype(np.float64))
+    E = np.where(amax > 0, E, 0).astype(np.int64)[:, None]
+    assert E.min() < -127
+    d = _digits_fixed_grid(hi, lo, E)
+    assert np.all(np.isfinite(d))
+    np.testing.assert_array_equal(d, _digits_twosum(hi, lo, E))
+    w = 2.0 ** (-8.0 * (np.arange(7) + 1))
+    rec = np.einsum("s,srk->rk", w, d.astype(np.float64))
+    np.testing.assert_array_equal(rec, np.ldexp(hi.astype(np.float64), -E))
