@@ -94,11 +94,13 @@ __device__ __forceinline__ C<R> row_reduce(C<R> y) {
   }
   return y;
 }
-constexpr int CU_TPR = 8;                // threads per row of k_colupd
+constexpr int CU_TPR = 1;                // threads per row of k_colupd (one panel column left to apply)
 constexpr int CU_ROWS = TR_NT / CU_TPR;  // rows per k_colupd block
 
-// A(i:n,i) -= V(i:n,0:jj) conj(W(i,0:jj))^T + W(i:n,0:jj) conj(V(i,0:jj))^T ;
-// d[i] = Re A(i,i) ; partial sums of |A(r,i)|^2 for r >= i+2.
+// A(i:n,i) -= V(i:n,cb:jj) conj(W(i,cb:jj))^T + W(i:n,cb:jj) conj(V(i,cb:jj))^T ;
+// d[i] = Re A(i,i) ; partial sums of |A(r,i)|^2 for r >= i+2.  The panel
+// columns below cb = c_begin were applied already by the previous column's
+// k_wcorr (which reads the same rows of V and W); here c_begin = jj - 1.
 // With fin != 0 it first completes the previous panel column jj-1 (the
 // zlatrd step w += alpha v, alpha = -1/2 tau (w^H v), from the partial sums
 // of k_wcorr): rows >= i+1 are written back by the block that owns them;
@@ -108,7 +110,7 @@ template <class R>
 __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
                                                   const int *nvec, int i, int k0, int jj, double *dd, int64_t sd,
                                                   double *nrm, int nrb, int fin, int nprev, z64 *scal,
-                                                  const z64 *wv) {
+                                                  const z64 *wv, int c_begin) {
   __shared__ C<R> sv[64], sw[64];
   __shared__ double red[32];
   __shared__ z64 s_alpha;
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t
   }
   __syncthreads();
   const C<R> alpha = fin ? cfrom64<R>(s_alpha) : cz<R>();
-  for (int c = threadIdx.x; c < jj; c += blockDim.x) {
+  for (int c = c_begin + threadIdx.x; c < jj; c += blockDim.x) {
     sv[c] = A[i + lda * (k0 + c)];
     C<R> wc = W[i + ldw * c];
     if (fin && c == jj - 1) {
@@ -154,7 +156,7 @@ __global__ void __launch_bounds__(TR_NT) k_colupd(C<R> *Ab, int64_t lda, int64_t
   C<R> acc = cz<R>();
   if (r < n) {
 #pragma unroll 4
-    for (int c = sub; c < jj; c += CU_TPR) {
+    for (int c = c_begin + sub; c < jj; c += CU_TPR) {
       C<R> wrc = W[r + ldw * c];
       if (fin && c == jj - 1) {
         cmac(wrc, alpha, A[r + lda * (i - 1)]);
@@ -397,41 +399,56 @@ __global__ void __launch_bounds__(TR_NT) k_dots(const C<R> *Ab, int64_t lda, int
 constexpr int WC_TPR = 8;
 constexpr int WC_ROWS = TR_NT / WC_TPR;  // rows per block
 template <class R>
-__global__ void __launch_bounds__(TR_NT) k_wcorr(const C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
+__global__ void __launch_bounds__(TR_NT) k_wcorr(C<R> *Ab, int64_t lda, int64_t sA, C<R> *Wb, int64_t sW,
                                                  const C<R> *Pb, int64_t sP, int64_t ldp, const int *nvec, int i,
                                                  int k0, int jj, const z64 *X, int ldx, const z64 *scal, z64 *wv,
-                                                 int nrb) {
-  __shared__ C<R> x1[64], x2[64];
+                                                 int nrb, int fuse) {
+  __shared__ C<R> x1[64], x2[64], nv[64], nw[64];
   __shared__ double red[32];
   const int b = blockIdx.y;
   const int n = nvec[b];
   if (i >= n - 1) return;
-  const C<R> *A = Ab + b * sA;
+  C<R> *A = Ab + b * sA;
   C<R> *W = Wb + b * sW;
   for (int c = threadIdx.x; c < jj; c += blockDim.x) {
     x1[c] = cfrom64<R>(X[b * ldx + c]);       // V^H v
     x2[c] = cfrom64<R>(X[b * ldx + jj + c]);  // W^H v
+    if (fuse) {                               // row i+1 of V and W
+      nv[c] = cconj(A[(i + 1) + lda * (k0 + c)]);
+      nw[c] = cconj(W[(i + 1) + lda * c]);
+    }
   }
   __syncthreads();
   const int sub = threadIdx.x % WC_TPR;
   const int r = i + 1 + blockIdx.x * WC_ROWS + threadIdx.x / WC_TPR;
   z64 part{0.0, 0.0};
   const int nch = cdiv_dev(n - i - 1, HV_CC);
-  C<R> y = cz<R>();
+  C<R> y = cz<R>(), nxt = cz<R>();
   if (r < n) {
     const C<R> *Pr = Pb + b * sP + r;
 #pragma unroll 4
     for (int ch = sub; ch < nch; ch += WC_TPR) y = cadd(y, Pr[(int64_t)ch * ldp]);
-    // this thread's share of the panel corrections, columns c = sub mod WC_TPR
+    // this thread's share of the panel corrections, columns c = sub mod
+    // WC_TPR; with fuse also the same columns' update of column i+1
     C<R> acc = cz<R>();
 #pragma unroll 4
     for (int c = sub; c < jj; c += WC_TPR) {
-      cmac(acc, W[r + lda * c], x1[c]);
-      cmac(acc, A[r + lda * (k0 + c)], x2[c]);
+      const C<R> wrc = W[r + lda * c], vrc = A[r + lda * (k0 + c)];
+      cmac(acc, wrc, x1[c]);
+      cmac(acc, vrc, x2[c]);
+      if (fuse) {
+        cmac(nxt, vrc, nw[c]);
+        cmac(nxt, wrc, nv[c]);
+      }
     }
     y = csub(y, cfin(acc));
   }
   y = row_reduce<R, WC_TPR>(y);
+  if (fuse) {
+    // A(r, i+1) -= V(r, 0:jj) conj(W(i+1, 0:jj))^T + W(r, 0:jj) conj(V(i+1, 0:jj))^T
+    nxt = row_reduce<R, WC_TPR>(cfin(nxt));
+    if (r < n && sub == 0) A[r + lda * (i + 1)] = csub(A[r + lda * (i + 1)], nxt);
+  }
   if (r < n && sub == 0) {
     const C<R> t = cfrom64<R>(scal[b * 4 + 1]);
     C<R> w = cmul(t, y);
@@ -559,7 +576,7 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
       const int fin = (jj > 0 && nprev > 0) ? 1 : 0;
       PP_KT(KT_COLUPD, s, (k_colupd<R><<<dim3(nparts, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, w.d, sd,
                                                                          w.nrm, w.nrb, fin, nprev, w.scal,
-                                                                         (z64 *)w.wv)));
+                                                                         (z64 *)w.wv, jj > 0 ? jj - 1 : 0)));
       nprev = 0;
       if (i >= nmax - 1) {
         count_launch(1);
@@ -574,8 +591,9 @@ cudaError_t tridiagonalize(EigWork &w, cudaStream_t s) {
       if (jj > 0) PP_KT(KT_DOTS, s, (k_dots<R><<<dim3(2 * jj, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb)));
       const int nr = cdiv(m, TR_NT);
       const int nrw = cdiv(m, WC_ROWS);
+      // within a panel, k_wcorr also applies columns 0 .. jj-1 to column i+1
       PP_KT(KT_WCORR, s, (k_wcorr<R><<<dim3(nrw, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, P, sP, lda, w.nvec, i, k0, jj, (z64 *)w.X, 2 * nb,
-                                               w.scal, (z64 *)w.wv, w.nrb)));
+                                               w.scal, (z64 *)w.wv, w.nrb, jj + 1 < jb ? 1 : 0)));
       if (jj == jb - 1 || i == nmax - 2) {
         // last column of the panel: the trailing update reads W next
         PP_KT(KT_WFIN, s, (k_wfin<R><<<dim3(nr, B), TR_NT, 0, s>>>(A, lda, sA, W, sW, w.nvec, i, jj, nrw, w.scal, (z64 *)w.wv, w.nrb)));
