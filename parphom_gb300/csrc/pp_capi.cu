@@ -576,7 +576,7 @@ int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_
     const bool can_tune = graphs_enabled() && !pp::kt_mask && !tc_stall_armed() && cs == cudaStreamCaptureStatusNone;
     if (t.split < 0 && !can_tune) t = Tuned{split_ways(), 6, 0.f};
     if (t.split < 0) {
-      // greedy: split over {4, 8, 16, 32} (at most B), then 4 instead of 6 mat-vec blocks per SM
+      // greedy: split over {4, 8, 16, 32} (at most B) with 6 mat-vec blocks per SM
       Tuned best{std::min(B, 8), 6, 1e30f};
       for (int sp : {4, 8, 16, 32}) {
         if (sp > B && sp != 4) continue;
@@ -584,9 +584,13 @@ int run_batch_graph(pp_ctx *c, int B, const pp_eig_opts *o, int mcap, bool want_
         const float ms = time_config(c, B, o, mcap, want_z, spc, 6);
         if (ms > 0.f && ms < best.ms) best = Tuned{spc, 6, ms};
       }
-      if (best.ms < 1e29f) {
-        const float ms = time_config(c, B, o, mcap, want_z, best.split, 4);
-        if (ms > 0.f && ms < best.ms) best = Tuned{best.split, 4, ms};
+      // then fewer persistent mat-vec blocks per SM (6 -> 4 -> 3 -> 2) while that helps:
+      // with several streams the mat-vecs of different parts share the SMs
+      for (int bps : {4, 3, 2}) {
+        if (best.ms > 1e29f) break;
+        const float ms = time_config(c, B, o, mcap, want_z, best.split, bps);
+        if (!(ms > 0.f && ms < best.ms)) break;
+        best = Tuned{best.split, bps, ms};
       }
       if (best.ms > 1e29f) best.ms = 0.f;
       t = best;
