@@ -321,7 +321,8 @@ size_t ws_bytes_estimate(int64_t n, int B, int mcap, int64_t nbnd, int64_t nbr) 
   size_t per = 16 * (size_t)n * n + 16 * (size_t)n * mcap + 8 * (size_t)5 * n * T + (size_t)n * T +
                16 * (size_t)n * 64 * 2 + 16 * (size_t)((n + 511) / 512) * 32 * std::max(mcap, 64) +
                16 * (size_t)((n + 63) / 64) * 32 * 32 + her2k_tc_bytes(n) + 8 * (size_t)(n + 128) +
-               8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd + 16 * (size_t)nbr * (n + mcap);
+               8 * 8 * 3 * (size_t)mcap + 16 * 3 * (size_t)nbnd + 16 * (size_t)nbr * (n + mcap) +
+               16 * 1024 * (size_t)std::max<int64_t>(1, (n + 30) / 32);  // compact-WY factors of all panels
   return per * B;
 }
 
